@@ -1,0 +1,286 @@
+"""Benchmark of the GB300 split-step propagator on the 256x256x2048 multipass-cell workload.
+
+One bench step = one pass of the cell (Cav = 0.5 m at 400 fixed split steps per pass, mirror
+lens at the end of the pass): 400 split steps over the 256x256x2048 complex64 field held in
+HBM.  value = grid-point-steps/s = Nx*Ny*Nt*400*K / (device time of K passes), timed with CUDA
+events on the stream the kernels run on, after W warm-up passes; the 1 GiB field is larger
+than L2, so no flush is needed between passes.  e2e = the same metric through the public C
+ABI with host buffers: every step uploads the complex128 field from pinned host memory
+(mpc_field_upload), runs the pass (mpc_run_fixed) and downloads it (mpc_field_download).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path for this workload -- the FP64 restatement in
+oracle/ (the reference's own FFTW/MPI build cannot be compiled; only plasma.c and a few
+propagation.c functions build, see oracle/build_ref.sh) -- with OpenMP on all host cores, each
+step a bounded sample of one split step of the same 256x256x2048 cell.
+Multi-GPU: the cells of a sweep are independent, so N > 1 runs N independent replicas
+(one cell per rank, no collective on the data path) and reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "grid-point-steps/s"
+STEPS_PER_PASS = 400
+BYTES_PER_PT_STEP = 32  # two compulsory complex64 sweeps (read + write) per split step
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch of the dominant sweep from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1])
+    return None
+
+
+def make_workload():
+    from mpc_gb300 import inputs
+    cfg = inputs.config2()
+    p, A = inputs.make_cell(cfg)
+    return cfg, p, A
+
+
+def cpu_baseline_run(p, A, nsteps: int, threads: int):
+    """The FP64 CPU restatement (oracle/) on `nsteps` split steps of the same cell."""
+    import oracle
+    oracle.set_threads(threads)
+    o = oracle.Oracle(p)
+    B = A.copy()
+    o.calibrate(B)
+    st = o.new_state()
+    t = time.perf_counter()
+    o.run_fixed(B, st, nsteps)
+    return time.perf_counter() - t
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_init()
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return
+    cfg, p, A = make_workload()
+    cores = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt = cpu_baseline_run(p, A, 1, cores)
+        if i >= args.warmup:
+            times.append(dt)
+    per = float(np.mean(times))
+    value = p.N * 1 / per
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "grid-point-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
+            "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror",
+                       "grid": [p.Nx, p.Ny, p.Nt], "sample": "1 split step per bench step"},
+            "cpu_baseline": {"value": value, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+                             "sample": "1 split step of the 256x256x2048 cell per bench step, FP64, OpenMP"},
+            "e2e": {"value": value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+
+
+def run_gb300(args):
+    rank, world, local, dist = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    from mpc_gb300 import capi
+    cfg, p, A = make_workload()
+    prop = capi.Propagator(p)
+    # pinned host field for the end-to-end path (physical units, calibrated)
+    pin = capi.PinnedArray(p.N)
+    pin.array[:] = A
+    prop.upload(pin.array, calibrate=True)
+    prop.sync()
+    pin.array[:] = prop.download()
+    stream = torch.cuda.ExternalStream(prop.stream_handle())
+
+    def one_pass():
+        prop.run_fixed(STEPS_PER_PASS)
+
+    for _ in range(args.warmup):
+        one_pass()
+    prop.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = prop.launch_count()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        one_pass()
+    ev1.record(stream)
+    ev1.synchronize()
+    launches = prop.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    pt_steps = p.N * STEPS_PER_PASS * args.steps
+    value = pt_steps * world / (ms / 1e3)
+
+    # per-sweep device time over one extra pass (events around every launch)
+    prop.profile(True)
+    one_pass()
+    kt = prop.kernel_times()
+    prop.profile(False)
+    hbm, src = peaks()
+    sweeps = {"pencil": (kt["pencil_ms"], kt["n_pencil"]), "plane": (kt["plane_ms"], kt["n_plane"])}
+    dom = max(sweeps, key=lambda k: sweeps[k][0])
+    dom_ms = sweeps[dom][0] / max(1, sweeps[dom][1])
+    bytes_launch = 16.0 * p.N  # one complex64 read + write of the whole field
+    achieved = bytes_launch / (dom_ms / 1e3) / 1e9
+    prof_name = {"pencil": "pencil_step_256x256x2048.txt", "plane": "plane_256x256x2048.txt"}[dom]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": profile_traffic(prof_name), "kernel": f"{dom} sweep",
+                "peak_source": src, "per_sweep_ms": {k: v[0] / max(1, v[1]) for k, v in sweeps.items()},
+                "step_frac_of_32B_floor": (value / world) * BYTES_PER_PT_STEP / (hbm * 1e9)}
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        prop.upload(pin.array)
+        one_pass()
+        prop.download(pin.array)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": p.N * STEPS_PER_PASS * e2e_steps * world / e2e_s, "unit": "grid-point-steps/s",
+           "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        nst = 1
+        dt = cpu_baseline_run(p, A, nst, cores)
+        cpu = {"value": p.N * nst / dt, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{nst} split step of the 256x256x2048 cell, FP64 oracle/ restatement, OpenMP"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+                "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
+                "config": {"workload": "multipass cell 256x256x2048, 400 fixed split steps per pass (1 pass = 1 step), "
+                                       "lens mirror, SST + ADK + plasma on", "grid": [p.Nx, p.Ny, p.Nt],
+                           "split_steps_per_step": STEPS_PER_PASS, "l2": "field 1 GiB > L2, no flush",
+                           "parallelism": f"replicas x{world}"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    prop.close()
+    pin.free()
+    if dist:
+        dist.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+/*
+ * mpc_gpu.h -- C ABI of the GB300 split-step propagator (libmpc_gpu.so).
+ *
+ * Drop-in boundary for the hot path of kmecseki/MPC: the entry points below replace the
+ * C functions declared in the reference's propagation.h and plasma.h, with the same
+ * argument meaning.  Differences, all deliberate:
+ *   - the six FFT plan handles of createPlans become one opaque context (mpc_ctx);
+ *   - every call returns an int status (MPC_OK = 0) and never exits the process;
+ *   - the physics is the reference's with its defects corrected (the design doc lists each);
+ *   - a device-resident field API (mpc_field_*, mpc_run_*) avoids the per-step host copies
+ *     the reference makes.
+ * Field layout everywhere: A[k*Nx*Ny + j*Nx + i] (i = x fastest, k = t slowest), complex128
+ * as interleaved doubles (the layout of cufftDoubleComplex), physical units as in MPC.c.
+ * One CUDA stream per context; a context is used from one host thread at a time.
+ */
+#ifndef MPC_GPU_H
+#define MPC_GPU_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MPC_OK = 0,
+    MPC_ERR_ARG = 1,        /* null pointer or invalid value */
+    MPC_ERR_SHAPE = 2,      /* grid shape not compiled into this library */
+    MPC_ERR_CUDA = 3,       /* a CUDA runtime call failed (mpc_last_error has the text) */
+    MPC_ERR_NOMEM = 4,      /* device allocation failed */
+    MPC_ERR_NONFINITE = 5,  /* the field became NaN/Inf */
+    MPC_ERR_STATE = 6,      /* call out of order (e.g. no field uploaded) */
+    MPC_ERR_IO = 7,         /* file could not be read/written */
+    MPC_ERR_UNSUPPORTED = 8 /* option not implemented on the device path */
+};
+
+enum { MPC_BOUNCE_SIGNFLIP = 0, MPC_BOUNCE_LENS = 1 };
+
+/* Run parameters: the param.bin record in the order MPC.c:77,180-203 reads it, plus
+ * the mirror model (the reference only has the diffraction sign flip). */
+typedef struct {
+    int dims[3];            /* Nx, Ny, Nt */
+    double dist, dzz;
+    const double *betas;    /* Nt, propagation constant beta(omega) - beta0 - beta1*omega, centred omega order */
+    double alpha, Cav, k0;
+    const double *wr;       /* Ny, centred transverse wavenumber grid (used for x and y) */
+    int sst_on;
+    const double *w;        /* Nt, centred angular-frequency offset grid */
+    double gamma2, w0;
+    int plasm;
+    double deltat, rho_c, rho_nt, n0, puls_e, Ab_M;
+    const double *r;        /* Ny, transverse positions */
+    double dr, def_err, dzmin, Esig;
+    char gas[9];
+    int bounce_mode;        /* MPC_BOUNCE_SIGNFLIP (reference) or MPC_BOUNCE_LENS */
+    double roc;             /* mirror radius of curvature [m], lens mode */
+} mpc_params;
+
+typedef struct mpc_ctx mpc_ctx;
+
+/* Library version string and the text of the last error on this thread. */
+const char *mpc_version(void);
+const char *mpc_last_error(void);
+/* 1 if kernels for this grid are compiled in. */
+int mpc_shape_supported(int Nx, int Ny, int Nt);
+
+/* Replaces createPlans (propagation.c:508-613): builds twiddle, frequency and phase tables
+ * and the device buffers for this grid.  The parameter arrays are copied. */
+int mpc_create(mpc_ctx **ctx, const mpc_params *p);
+int mpc_destroy(mpc_ctx *ctx);
+
+/* One symmetric split step L(dzz/2) N(dzz) L(dzz/2) on a host complex128 field, in place
+ * (propagation.c:111-372, ssfmprop).  signmem, puls_e, BP1 (Nx), BP2 (Ny), y1[4], y2[4],
+ * bps1, bps2 are updated as the reference updates them; the beam diagnostics (BP1, BP2,
+ * y1, y2, bps1, bps2) only when change == 1. */
+int mpc_ssfmprop(mpc_ctx *ctx, double *A, int sst_on, double dzz, int *signmem, double z,
+                 double *puls_e, double *BP1, double *BP2, double *y1, double *y2,
+                 double *bps1, double *bps2, int change);
+
+/* Linear step on a host complex128 field with caller tables (propagation.c:3-108):
+ * exp_D0[Nt] in FFT order (after fftshift), expR[Nx] in the order the corrected
+ * calcexpR returns it (FFT order), applied as conj(expR) along y and x. */
+int mpc_linearstep(mpc_ctx *ctx, double *A, const double *exp_D0, const double *expR);
+
+/* Diffraction table (propagation.c:375-391, corrected: imaginary exponent, FFT order,
+ * centre wr[N/2]) into expR[Nx] (complex128); updates *signmem like the reference. */
+int mpc_calcexpR(mpc_ctx *ctx, double *expR, int *signmem, double z, double dzz);
+
+/* Ionization (plasma.c:118-245, corrected): tau_c[N] and freeelectrons_sp[N] (FP64) for a
+ * host complex128 field, computed on the device. */
+int mpc_ioniz(mpc_ctx *ctx, const double *A, double *tau_c, double *freeelectrons_sp);
+
+/* ADK rates (plasma.c:43-58) of both ionization stages for n field values E (atomic units),
+ * corrected constants of plasma.c:264-287 for the context's gas, computed on the device. */
+int mpc_ADK(mpc_ctx *ctx, long n, const double *E, double *rates1, double *rates2);
+
+/* 1/e^2 beam size from a beam profile BP[n] and positions r[n] (propagation.c:460-504):
+ * *vald1oes = r[p2] - r[p1], y = {r[p1], r[p2], BP[p1], BP[p2]}.  Host scalar search. */
+int mpc_calc1oes(const double *BP, int n, const double *r, double *vald1oes, double *y);
+
+/* Step-size control (propagation.c:616-677): err = |C2-C1|/|C2| reduced on the device,
+ * then the reference's dz rule.  C1, C2 host complex128 fields. */
+int mpc_setStep(mpc_ctx *ctx, double *dzz, const double *C1, const double *C2,
+                const double *y1, const double *y2, int *bad, double *err);
+
+/* ---- device-resident field (the fast path) ---------------------------------------- */
+/* Upload / download a host complex128 field (physical units); upload optionally applies
+ * the energy calibration of MPC.c:206-216 (both parts scaled). */
+int mpc_field_upload(mpc_ctx *ctx, const double *A, int calibrate);
+int mpc_field_download(mpc_ctx *ctx, double *A);
+
+/* Run state of the device-resident loop (MPC.c:234-238). */
+typedef struct {
+    double z, dzz, err, puls_e, bps1, bps2;
+    int signmem, bad, nstep, attempts;
+    double y1[4], y2[4];
+} mpc_state;
+int mpc_get_state(mpc_ctx *ctx, mpc_state *st);
+int mpc_set_state(mpc_ctx *ctx, const mpc_state *st);
+
+/* nsteps fixed split steps of length state.dzz on the device-resident field, merging the
+ * half linear steps of consecutive steps; mirror bounces (lens phase or diffraction sign
+ * flip) at every multiple of Cav.  Updates state.z, nstep, puls_e. */
+int mpc_run_fixed(mpc_ctx *ctx, int nsteps);
+
+/* Diagnostics of the device-resident field (MPC.c:389-449, propagation.c:343-361):
+ * temp[Nt] = sum_xy |A|^2, spec[Nt] = sum_xy |FFT_t A|^2 (FFT order), BP1[Nx], BP2[Ny];
+ * any pointer may be NULL. */
+int mpc_diag(mpc_ctx *ctx, double *temp, double *spec, double *BP1, double *BP2);
+
+/* Total energy sum |A|^2 dx dy dt hbar w0 of the device-resident field (FP64 reduction). */
+int mpc_energy(mpc_ctx *ctx, double *energy);
+
+/* Synchronise the context's stream; returns MPC_ERR_CUDA on an asynchronous fault. */
+int mpc_sync(mpc_ctx *ctx);
+
+/* ---- measurement and host buffers (no counterpart in the reference) ---------------- */
+/* Page-locked host buffer for fast host<->device copies of the field. */
+int mpc_host_alloc(void **ptr, size_t bytes);
+int mpc_host_free(void *ptr);
+/* The cudaStream_t every kernel of this context is launched on. */
+int mpc_stream_handle(mpc_ctx *ctx, void **stream);
+/* Number of kernels this context has launched so far. */
+long mpc_launch_count(mpc_ctx *ctx);
+/* With on != 0, every pencil and plane sweep is bracketed by CUDA events on the context's
+ * stream; mpc_kernel_times sums their durations since the last enable (synchronises). */
+int mpc_profile(mpc_ctx *ctx, int on);
+int mpc_kernel_times(mpc_ctx *ctx, double *pencil_ms, long *n_pencil, double *plane_ms, long *n_plane);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

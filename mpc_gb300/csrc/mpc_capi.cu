@@ -1,0 +1,1026 @@
+// mpc_capi.cu -- host side of libmpc_gpu.so: the C ABI of include/mpc_gpu.h.
+//
+// The context owns the device-resident field (complex64, slot layout, see mpc_kernels.cuh),
+// the FFT twiddles and position->frequency tables of the three axes, the per-step phase
+// tables (computed on the device in FP64 and rounded to complex64) and the scratch of the
+// pencil sweep.  Every entry point returns an int status; CUDA errors are reported through
+// mpc_last_error().  Host code only sequences kernels and evaluates scalar control logic
+// (pass sign, step-size rule); all per-point arithmetic runs on the GPU.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/mpc_gpu.h"
+#include "mpc_shapes.cuh"
+
+using mpc::NLConst;
+using mpc::PencilArgs;
+using mpc::PlaneArgs;
+using mpc::PlaneTables;
+using mpc::ShapeOps;
+
+namespace mpc {
+extern const ShapeOps* const shape_list_a[];
+extern const ShapeOps* const shape_list_b[];
+extern const ShapeOps* const shape_list_c[];
+extern const ShapeOps* const shape_list_d[];
+}  // namespace mpc
+
+// constants.h:1-11
+static const double ZW0 = 377.0, NC = 1.0, FCTR = 0.89, IH = 27.21, EF = 5.14220642e11;
+static const double ME = 9.1094e-31, EL0 = 1.602e-19, NAVO = 6.02214e+23, T0 = 2.4188843265e-17;
+static const double C0 = 299792458.0, HBAR = 1.054560652926899e-34;
+// device units: |a|^2 = intensity / I_UNIT
+static const double I_UNIT = 1e16;
+
+static thread_local std::string g_err;
+static int fail(int code, const char* what, cudaError_t e = cudaSuccess) {
+    char buf[512];
+    if (e != cudaSuccess) snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    else snprintf(buf, sizeof buf, "%s", what);
+    g_err = buf;
+    return code;
+}
+#define CK(call, what)                                    \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return fail(MPC_ERR_CUDA, what, _e); \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// small device kernels: tables, reductions, element-wise ADK
+// ---------------------------------------------------------------------------------------
+struct TabIn {
+    const double* wr;     // centred k grid (Nx == Ny entries)
+    const double* betas;  // centred, Nt
+    const int* fx;        // position -> FFT frequency index
+    const int* fy;
+    const int* ft;
+    int Nx, Ny, Nt;
+    double zd, zp, k0, alpha, scale;
+};
+
+// Rx[px] = exp(-i zd kap^2/(2 k0)), kap = wr[m] - wr[N/2], m = centred index of freq(px);
+// D[pos] = scale * exp(zp (i beta[m] - alpha/2)).  Phase arguments and their range
+// reduction in FP64 (propagation.c:375-391, kernels.cu:47-54, corrected).
+__global__ void k_tables(TabIn in, float2* Rx, float2* Ry, float2* D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < in.Nx) {
+        const int m = (in.fx[i] + in.Nx / 2) % in.Nx;
+        const double kap = in.wr[m] - in.wr[in.Nx / 2];
+        double s, c;
+        sincos(-in.zd * kap * kap / (2.0 * in.k0), &s, &c);
+        Rx[i] = make_float2((float)c, (float)s);
+    }
+    if (i < in.Ny) {
+        const int m = (in.fy[i] + in.Ny / 2) % in.Ny;
+        const double kap = in.wr[m] - in.wr[in.Ny / 2];
+        double s, c;
+        sincos(-in.zd * kap * kap / (2.0 * in.k0), &s, &c);
+        Ry[i] = make_float2((float)c, (float)s);
+    }
+    if (i < in.Nt) {
+        const int m = (in.ft[i] + in.Nt / 2) % in.Nt;
+        const double amp = exp(-in.zp * in.alpha / 2.0) * in.scale;
+        double s, c;
+        sincos(in.zp * in.betas[m], &s, &c);
+        D[i] = make_float2((float)(amp * c), (float)(amp * s));
+    }
+}
+
+// exp(-i k0 r^2 / roc) for the mirror lens (lens bounce mode)
+__global__ void k_lens(const double* r, int n, double k0, double roc, float2* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        double s, c;
+        sincos(-k0 * r[i] * r[i] / roc, &s, &c);
+        out[i] = make_float2((float)c, (float)s);
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    v = (threadIdx.x < blockDim.x / 32) ? sh[threadIdx.x] : 0.0;
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// sum |x|^2 of a complex64 array (FP32 per thread over a short run, FP64 across)
+__global__ void k_norm2_c64(const float2* __restrict__ x, long n, double* out) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float2 v = x[i];
+        acc += (double)fmaf(v.x, v.x, v.y * v.y);
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) atomicAdd(out, acc);
+}
+
+// sum |a-b|^2 and sum |b|^2 of two complex128 arrays (setStep, propagation.c:624-633)
+__global__ void k_diffnorm_c128(const double2* __restrict__ a, const double2* __restrict__ b, long n, double* out) {
+    __shared__ double sh[32];
+    double s1 = 0.0, s2 = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double2 u = a[i], v = b[i];
+        const double dx = v.x - u.x, dy = v.y - u.y;
+        s1 += dx * dx + dy * dy;
+        s2 += v.x * v.x + v.y * v.y;
+    }
+    s1 = block_sum(s1, sh);
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) {
+        atomicAdd(out, s1);
+        atomicAdd(out + 1, s2);
+    }
+}
+
+// spec[freq(pos)] = scale * sum_q |S[pos, q]|^2 for the slot layout; one block per slot
+__global__ void k_spec(const float2* __restrict__ S, int NP, int SLO, const int* ft, double scale, double* spec) {
+    __shared__ double sh[32];
+    const int pos = blockIdx.x;
+    double acc = 0.0;
+    const size_t base = (size_t)(pos / SLO) * NP * SLO + (pos % SLO);
+    for (int q = threadIdx.x; q < NP; q += blockDim.x) {
+        const float2 v = S[base + (size_t)q * SLO];
+        acc += (double)fmaf(v.x, v.x, v.y * v.y);
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) spec[ft[pos]] = acc * scale;
+}
+
+// BP1[x] = sum_y E[y*Nx + x], BP2[y] = sum_x E[y*Nx + x] from per-pencil sums E
+__global__ void k_beam_profiles(const double* E, int Nx, int Ny, double* BP1, double* BP2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < Nx) {
+        double s = 0.0;
+        for (int y = 0; y < Ny; y++) s += E[(size_t)y * Nx + i];
+        BP1[i] = s;
+    }
+    if (i < Ny) {
+        double s = 0.0;
+        for (int x = 0; x < Nx; x++) s += E[(size_t)i * Nx + x];
+        BP2[i] = s;
+    }
+}
+
+struct ADKConst {
+    double Kon1, Kon2, Kon3, Kon4, Kon5, Kon6;
+};
+// plasma.c:43-58 in FP64
+__global__ void k_adk(long n, const double* __restrict__ E, double* r1, double* r2, ADKConst k) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double e = E[i];
+        r1[i] = k.Kon1 * pow(k.Kon3 / e, k.Kon5) * exp(-k.Kon3 / (3.0 * e));
+        r2[i] = k.Kon2 * pow(k.Kon4 / e, k.Kon6) * exp(-k.Kon4 / (3.0 * e));
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------
+struct TableSet {
+    float2* Rx = nullptr;
+    float2* Ry = nullptr;
+    float2* D = nullptr;
+};
+
+struct mpc_ctx {
+    const ShapeOps* ops = nullptr;
+    int Nx = 0, Ny = 0, Nt = 0;
+    long NP = 0, N = 0;
+    mpc_params p{};
+    std::vector<double> betas, wr, w, r;
+    double fs = 1.0;    // device units per physical field unit
+    NLConst nl{};
+    float sst_c_full = 0.0f;  // self-steepening prefactor when switched on
+    int ion_gas_ok = 0;
+    double I1 = 0, I2 = 0;
+    ADKConst adk{};
+    cudaStream_t st = nullptr;
+    int nsm = 0, pencil_grid = 0, plane_clusters = 0;
+    float2* S = nullptr;        // state, slot layout
+    float2* scratch = nullptr;
+    double2* io = nullptr;      // complex128 staging, N
+    double2* io2 = nullptr;     // second complex128 staging (setStep)
+    float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;
+    float* wpos = nullptr;
+    int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
+    std::vector<int> hfx, hfy, hft;
+    double *dwr = nullptr, *dbetas = nullptr, *dr = nullptr;
+    float2 *lensx = nullptr, *lensy = nullptr;
+    double* penergy = nullptr;  // NP
+    double* dred = nullptr;     // reduction outputs (2 Nt + Nx + Ny + 64 doubles)
+    std::map<std::tuple<double, double, double>, TableSet> tables;
+    TableSet ident;             // identity tables (zd = zp = 0, scale 1/(NxNy))
+    mpc_state state{};
+    int have_field = 0;
+    long launches = 0;          // kernels launched by this context
+    int profiling = 0;          // bracket sweeps with events
+    struct Ev { int kind; cudaEvent_t a, b; };
+    std::vector<Ev> events;     // kind 0 = pencil sweep, 1 = plane sweep
+};
+
+static void prof_begin(mpc_ctx* c, int kind, cudaEvent_t* a) {
+    (void)kind;
+    *a = nullptr;
+    if (!c->profiling) return;
+    cudaEventCreate(a);
+    cudaEventRecord(*a, c->st);
+}
+static void prof_end(mpc_ctx* c, int kind, cudaEvent_t a) {
+    if (!c->profiling || !a) return;
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, c->st);
+    c->events.push_back(mpc_ctx::Ev{kind, a, b});
+}
+static void prof_clear(mpc_ctx* c) {
+    for (auto& e : c->events) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    c->events.clear();
+}
+
+static const ShapeOps* find_shape(int Nx, int Ny, int Nt) {
+    const ShapeOps* const* lists[] = {mpc::shape_list_a, mpc::shape_list_b, mpc::shape_list_c, mpc::shape_list_d};
+    for (auto l : lists)
+        for (int i = 0; l[i]; i++)
+            if (l[i]->Nx == Nx && l[i]->Ny == Ny && l[i]->Nt == Nt) return l[i];
+    return nullptr;
+}
+
+// Position -> FFT frequency index of the in-place DIF sweep with radices 16,...,16,r_last
+// (mpc_fft.cuh): pos = sum_s span_s k_s, freq = k_1 + r_1 k_2 + r_1 r_2 k_3 + ...
+static std::vector<int> freq_of_pos(int N) {
+    std::vector<int> radix, span;
+    for (int L = N; L > 1;) {
+        const int R = (L >= 16) ? 16 : L;
+        radix.push_back(R);
+        span.push_back(L / R);
+        L /= R;
+    }
+    std::vector<int> f(N);
+    for (int pos = 0; pos < N; pos++) {
+        int rem = pos, freq = 0, mult = 1;
+        for (size_t s = 0; s < radix.size(); s++) {
+            const int k = rem / span[s];
+            rem -= k * span[s];
+            freq += k * mult;
+            mult *= radix[s];
+        }
+        f[pos] = freq;
+    }
+    return f;
+}
+
+static int upload_twiddles(int N, float2** d) {
+    std::vector<float2> h(N);
+    for (int k = 0; k < N; k++) {
+        const double a = -2.0 * M_PI * (double)k / (double)N;
+        h[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    CK(cudaMalloc(d, sizeof(float2) * N), "cudaMalloc twiddles");
+    CK(cudaMemcpy(*d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "copy twiddles");
+    return MPC_OK;
+}
+
+static int pass_sign(double z, double Cav) { return ((int)(floor(z / Cav) + 1) % 2) * 2 - 1; }
+
+// ionizpot (plasma.c:4-40) and Natoms (plasma.c:61-115)
+static int gas_tables(const char* gas, double* I1, double* I2, double* Natm, double* sig) {
+    struct G { const char* n; double i1, i2, dens, M, sig; };
+    static const G g[] = {
+        {"Argon", 15.75962, 27.62967, 1.784 * 1e3, 39.941, 1.57e-20},
+        {"Helium", 24.58741, 54.41778, 0.166e3, 4.002602, 6.11e-20},
+        {"Neon", 21.5646, 40.96328, 0.9002e3, 20.1797, 1.65e-20},
+        {"Air", 0.78084 * 14.53414 + 0.20946 * 13.61806 + 0.00934 * 15.75962,
+         0.78084 * 29.6013 + 0.20946 * 35.11730 + 0.00934 * 27.62967, 1.205e3, 28.97, 10e-20},
+        {"Nitrogen", 14.53414, 29.6013, 1.65e3, 14.0067, 10.2e-20},
+        {"Xenon", 12.1298, 21.20979, 5.86e3, 5.761, 3.55e-20},
+        {"Krypton", 13.99961, 24.35985, 3.749e3, 83.798, 1.15e-20},
+    };
+    for (const G& e : g)
+        if (strcmp(gas, e.n) == 0) {
+            *I1 = e.i1;
+            *I2 = e.i2;
+            *Natm = e.dens * NAVO / e.M;
+            *sig = e.sig;
+            return 1;
+        }
+    return 0;
+}
+
+// FP32 constants of the fused nonlinear step (plasma.c:118-245, propagation.c:244-327;
+// A11 and A18 corrections applied)
+static void build_nl(mpc_ctx* c) {
+    const mpc_params& p = c->p;
+    NLConst& n = c->nl;
+    memset(&n, 0, sizeof n);
+    const double fs2 = c->fs * c->fs;
+    n.gam = (float)(p.gamma2 / fs2);
+    c->sst_c_full = (float)(p.gamma2 / (p.w0 * fs2));
+    n.sst_c = p.sst_on == 1 ? c->sst_c_full : 0.0f;
+    n.I_scale = (float)I_UNIT;
+    n.E_c = (float)(sqrt(2.0 * ZW0 / NC) * FCTR / EF);
+    double I1 = 0, I2 = 0, Natm = 0, sig = 0;
+    c->ion_gas_ok = gas_tables(p.gas, &I1, &I2, &Natm, &sig);
+    c->I1 = I1;
+    c->I2 = I2;
+    const double Iion[2] = {I1 / IH, I2 / IH};
+    const double nq[2] = {1.0 / sqrt(2.0 * Iion[0]), 2.0 / sqrt(2.0 * Iion[1])};
+    double K1[2], K3[2], K5[2];
+    for (int s = 0; s < 2; s++) {
+        const double Cnl = sqrt(pow(2.0, 2.0 * nq[s]) / (nq[s] * tgamma(nq[s] + 1.0) * tgamma(nq[s])));
+        K1[s] = Cnl * Cnl * sqrt(6.0 / M_PI) * 1.0 * Iion[s];
+        K3[s] = 2.0 * pow(2.0 * Iion[s], 1.5);
+        K5[s] = 2.0 * nq[s] - 0.0 - 1.5;
+        n.lnK1[s] = (float)log(K1[s]);
+        n.K3[s] = (float)K3[s];
+        n.lnK3[s] = (float)log(K3[s]);
+        n.K5[s] = (float)K5[s];
+    }
+    c->adk = ADKConst{K1[0], K1[1], K3[0], K3[1], K5[0], K5[1]};
+    n.Kon = (float)(p.deltat / T0);
+    n.ve_c = (float)(EL0 * EF / (sqrt(2.0) * ME * p.w0));
+    n.K3c = (float)(sig * p.rho_nt);
+    const double k0ion = p.w0 / C0;  // plasma.c:141
+    n.K4w0 = (float)(k0ion / (p.n0 * p.rho_c) * p.w0 * p.w0);
+    n.w0sq = (float)(p.w0 * p.w0);
+    n.inv_w0 = (float)(1.0 / p.w0);
+    n.inv_I1 = I1 > 0 ? (float)(1.0 / I1) : 0.0f;
+    n.rho_half = (float)(p.rho_nt / 2.0);
+    n.plasma = (p.plasm == 1) ? 1 : 0;
+}
+
+static int get_tables(mpc_ctx* c, double zd, double zp, double scale, TableSet* out) {
+    auto key = std::make_tuple(zd, zp, scale);
+    auto it = c->tables.find(key);
+    if (it != c->tables.end()) {
+        *out = it->second;
+        return MPC_OK;
+    }
+    if (c->tables.size() > 64) {  // adaptive runs: recycle the cache
+        cudaStreamSynchronize(c->st);
+        for (auto& kv : c->tables) {
+            cudaFree(kv.second.Rx);
+        }
+        c->tables.clear();
+    }
+    TableSet t;
+    float2* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(float2) * (c->Nx + c->Ny + c->Nt)), "cudaMalloc tables");
+    t.Rx = buf;
+    t.Ry = buf + c->Nx;
+    t.D = buf + c->Nx + c->Ny;
+    TabIn in{c->dwr, c->dbetas, c->dfx, c->dfy, c->dft, c->Nx, c->Ny, c->Nt, zd, zp, c->p.k0, c->p.alpha, scale};
+    const int n = c->Nt > c->Nx ? c->Nt : c->Nx;
+    k_tables<<<(n + 255) / 256, 256, 0, c->st>>>(in, (float2*)t.Rx, (float2*)t.Ry, (float2*)t.D);
+    CK(cudaGetLastError(), "k_tables");
+    c->launches++;
+    c->tables[key] = t;
+    *out = t;
+    return MPC_OK;
+}
+
+static int launch_pencil(mpc_ctx* c, int mode, PencilArgs a) {
+    a.scratch = c->scratch;
+    a.tw = c->twt;
+    a.wpos = c->wpos;
+    a.NP = (int)c->NP;
+    a.ntiles = (int)(c->NP / c->ops->P);
+    cudaEvent_t ev;
+    prof_begin(c, 0, &ev);
+    CK(c->ops->pencil(mode, a, c->pencil_grid, c->st), "pencil kernel launch");
+    prof_end(c, 0, ev);
+    c->launches++;
+    return MPC_OK;
+}
+
+static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSet& t1, const TableSet* t2) {
+    PlaneArgs a{};
+    a.in = in;
+    a.out = out;
+    a.twx = c->twx;
+    a.twy = c->twy;
+    a.t1 = PlaneTables{t1.Rx, t1.Ry, t1.D};
+    if (t2) {
+        a.t2 = PlaneTables{t2->Rx, t2->Ry, t2->D};
+        a.lens = 1;
+    } else {
+        a.t2 = a.t1;
+        a.lens = 0;
+    }
+    a.lensx = c->lensx;
+    a.lensy = c->lensy;
+    a.NP = (int)c->NP;
+    a.nunits = c->ops->SLO == 2 ? c->Nt / 2 : c->Nt / c->ops->PB;
+    cudaEvent_t ev;
+    prof_begin(c, 1, &ev);
+    CK(c->ops->plane(a, c->plane_clusters, c->st), "plane kernel launch");
+    prof_end(c, 1, ev);
+    c->launches++;
+    return MPC_OK;
+}
+
+static int ensure_io(mpc_ctx* c, int which) {
+    double2** b = which == 0 ? &c->io : &c->io2;
+    if (!*b) {
+        if (cudaMalloc(b, sizeof(double2) * c->N) != cudaSuccess) {
+            *b = nullptr;
+            return fail(MPC_ERR_NOMEM, "cudaMalloc complex128 staging");
+        }
+    }
+    return MPC_OK;
+}
+
+extern "C" {
+
+const char* mpc_version(void) { return "mpc_gb300 0.1 (sm_103a)"; }
+const char* mpc_last_error(void) { return g_err.c_str(); }
+int mpc_shape_supported(int Nx, int Ny, int Nt) { return find_shape(Nx, Ny, Nt) ? 1 : 0; }
+
+int mpc_destroy(mpc_ctx* c) {
+    if (!c) return MPC_OK;
+    if (c->st) cudaStreamSynchronize(c->st);
+    prof_clear(c);
+    for (auto& kv : c->tables) cudaFree(kv.second.Rx);
+    if (c->ident.Rx) cudaFree(c->ident.Rx);
+    void* ptrs[] = {c->S, c->scratch, c->io, c->io2, c->twx, c->twy, c->twt, c->wpos, c->dfx, c->dfy,
+                    c->dft, c->dwr, c->dbetas, c->dr, c->lensx, c->lensy, c->penergy, c->dred};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return MPC_OK;
+}
+
+int mpc_create(mpc_ctx** out, const mpc_params* p) {
+    if (!out || !p) return fail(MPC_ERR_ARG, "null argument");
+    *out = nullptr;
+    const int Nx = p->dims[0], Ny = p->dims[1], Nt = p->dims[2];
+    if (Nx != Ny) return fail(MPC_ERR_SHAPE, "the k grid wr of param.bin serves both x and y: Nx must equal Ny");
+    const ShapeOps* ops = find_shape(Nx, Ny, Nt);
+    if (!ops) return fail(MPC_ERR_SHAPE, "grid shape not compiled into libmpc_gpu");
+    if (!p->betas || !p->wr || !p->w || !p->r) return fail(MPC_ERR_ARG, "null parameter array");
+    if (!(p->k0 > 0) || !(p->w0 > 0) || !(p->Cav > 0)) return fail(MPC_ERR_ARG, "k0, w0 and Cav must be positive");
+    mpc_ctx* c = new mpc_ctx();
+    c->ops = ops;
+    c->Nx = Nx;
+    c->Ny = Ny;
+    c->Nt = Nt;
+    c->NP = (long)Nx * Ny;
+    c->N = c->NP * Nt;
+    c->p = *p;
+    c->betas.assign(p->betas, p->betas + Nt);
+    c->wr.assign(p->wr, p->wr + Ny);
+    c->w.assign(p->w, p->w + Nt);
+    c->r.assign(p->r, p->r + Ny);
+    c->p.betas = c->betas.data();
+    c->p.wr = c->wr.data();
+    c->p.w = c->w.data();
+    c->p.r = c->r.data();
+    c->p.gas[8] = 0;
+    c->fs = sqrt(HBAR * p->w0 / I_UNIT);
+    build_nl(c);
+    int rc;
+#define TRY(x)                      \
+    if ((rc = (x)) != MPC_OK) {     \
+        mpc_destroy(c);             \
+        return rc;                  \
+    }
+#define TRYC(x, what)                                  \
+    {                                                  \
+        cudaError_t _e = (x);                          \
+        if (_e != cudaSuccess) {                       \
+            mpc_destroy(c);                            \
+            return fail(MPC_ERR_CUDA, what, _e);       \
+        }                                              \
+    }
+    int dev = 0;
+    TRYC(cudaGetDevice(&dev), "cudaGetDevice");
+    TRYC(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    TRYC(ops->setup(), "kernel attribute setup");
+    TRYC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
+    const int ntiles = (int)(c->NP / ops->P);
+    c->pencil_grid = ntiles < c->nsm ? ntiles : c->nsm;
+    const int nunits = ops->SLO == 2 ? Nt / 2 : Nt / ops->PB;
+    int mc = ops->max_clusters();
+    if (mc <= 0) {
+        mpc_destroy(c);
+        return fail(MPC_ERR_CUDA, "plane cluster configuration cannot be scheduled on this device");
+    }
+    c->plane_clusters = mc < nunits ? mc : nunits;
+    if (cudaMalloc(&c->S, sizeof(float2) * c->N) != cudaSuccess) {
+        mpc_destroy(c);
+        return fail(MPC_ERR_NOMEM, "cudaMalloc field");
+    }
+    TRYC(cudaMalloc(&c->scratch, sizeof(float2) * (size_t)c->pencil_grid * mpc::kTilePoints), "cudaMalloc scratch");
+    TRY(upload_twiddles(Nx, &c->twx));
+    TRY(upload_twiddles(Ny, &c->twy));
+    TRY(upload_twiddles(Nt, &c->twt));
+    c->hfx = freq_of_pos(Nx);
+    c->hfy = freq_of_pos(Ny);
+    c->hft = freq_of_pos(Nt);
+    TRYC(cudaMalloc(&c->dfx, sizeof(int) * (Nx + Ny + Nt)), "cudaMalloc freq tables");
+    c->dfy = c->dfx + Nx;
+    c->dft = c->dfy + Ny;
+    TRYC(cudaMemcpy(c->dfx, c->hfx.data(), sizeof(int) * Nx, cudaMemcpyHostToDevice), "copy fx");
+    TRYC(cudaMemcpy(c->dfy, c->hfy.data(), sizeof(int) * Ny, cudaMemcpyHostToDevice), "copy fy");
+    TRYC(cudaMemcpy(c->dft, c->hft.data(), sizeof(int) * Nt, cudaMemcpyHostToDevice), "copy ft");
+    {
+        // omega of each t position: wbuff = fftshift(w) (propagation.c:170-177) indexed by freq(pos)
+        std::vector<float> wp(Nt);
+        for (int pos = 0; pos < Nt; pos++) wp[pos] = (float)c->w[(c->hft[pos] + Nt / 2) % Nt];
+        TRYC(cudaMalloc(&c->wpos, sizeof(float) * Nt), "cudaMalloc wpos");
+        TRYC(cudaMemcpy(c->wpos, wp.data(), sizeof(float) * Nt, cudaMemcpyHostToDevice), "copy wpos");
+    }
+    TRYC(cudaMalloc(&c->dwr, sizeof(double) * (Ny + Nt + Ny)), "cudaMalloc FP64 grids");
+    c->dbetas = c->dwr + Ny;
+    c->dr = c->dbetas + Nt;
+    TRYC(cudaMemcpy(c->dwr, c->wr.data(), sizeof(double) * Ny, cudaMemcpyHostToDevice), "copy wr");
+    TRYC(cudaMemcpy(c->dbetas, c->betas.data(), sizeof(double) * Nt, cudaMemcpyHostToDevice), "copy betas");
+    TRYC(cudaMemcpy(c->dr, c->r.data(), sizeof(double) * Ny, cudaMemcpyHostToDevice), "copy r");
+    TRYC(cudaMalloc(&c->lensx, sizeof(float2) * (Nx + Ny)), "cudaMalloc lens");
+    c->lensy = c->lensx + Nx;
+    if (p->bounce_mode == MPC_BOUNCE_LENS && p->roc != 0.0) {
+        k_lens<<<(Nx + 255) / 256, 256, 0, c->st>>>(c->dr, Nx, p->k0, p->roc, c->lensx);
+        k_lens<<<(Ny + 255) / 256, 256, 0, c->st>>>(c->dr, Ny, p->k0, p->roc, c->lensy);
+        TRYC(cudaGetLastError(), "k_lens");
+    }
+    TRYC(cudaMalloc(&c->penergy, sizeof(double) * c->NP), "cudaMalloc pencil energies");
+    // reductions: temp [0, Nt), spec [Nt, 2 Nt), beam profiles and sums use the front
+    TRYC(cudaMalloc(&c->dred, sizeof(double) * (2 * Nt + Nx + Ny + 64)), "cudaMalloc reductions");
+    {
+        float2* buf = nullptr;
+        TRYC(cudaMalloc(&buf, sizeof(float2) * (Nx + Ny + Nt)), "cudaMalloc identity tables");
+        c->ident = TableSet{buf, buf + Nx, buf + Nx + Ny};
+        TabIn in{c->dwr, c->dbetas, c->dfx, c->dfy, c->dft, Nx, Ny, Nt, 0.0, 0.0, p->k0, p->alpha,
+                 1.0 / (double)c->NP};
+        const int n = Nt > Nx ? Nt : Nx;
+        k_tables<<<(n + 255) / 256, 256, 0, c->st>>>(in, buf, buf + Nx, buf + Nx + Ny);
+        TRYC(cudaGetLastError(), "k_tables identity");
+    }
+    TRYC(cudaStreamSynchronize(c->st), "context setup");
+    c->state.dzz = p->dzz;
+    c->state.puls_e = p->puls_e;
+    c->state.signmem = 1;
+#undef TRY
+#undef TRYC
+    *out = c;
+    return MPC_OK;
+}
+
+int mpc_sync(mpc_ctx* c) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    CK(cudaStreamSynchronize(c->st), "stream synchronize");
+    return MPC_OK;
+}
+
+int mpc_host_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return fail(MPC_ERR_ARG, "null argument");
+    *ptr = nullptr;
+    cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e != cudaSuccess) return fail(MPC_ERR_NOMEM, "cudaMallocHost", e);
+    return MPC_OK;
+}
+
+int mpc_host_free(void* ptr) {
+    if (ptr) CK(cudaFreeHost(ptr), "cudaFreeHost");
+    return MPC_OK;
+}
+
+int mpc_stream_handle(mpc_ctx* c, void** stream) {
+    if (!c || !stream) return fail(MPC_ERR_ARG, "null argument");
+    *stream = (void*)c->st;
+    return MPC_OK;
+}
+
+long mpc_launch_count(mpc_ctx* c) { return c ? c->launches : -1; }
+
+int mpc_profile(mpc_ctx* c, int on) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    CK(cudaStreamSynchronize(c->st), "profile sync");
+    prof_clear(c);
+    c->profiling = on ? 1 : 0;
+    return MPC_OK;
+}
+
+int mpc_kernel_times(mpc_ctx* c, double* pencil_ms, long* n_pencil, double* plane_ms, long* n_plane) {
+    if (!c || !pencil_ms || !n_pencil || !plane_ms || !n_plane) return fail(MPC_ERR_ARG, "null argument");
+    CK(cudaStreamSynchronize(c->st), "profile sync");
+    *pencil_ms = *plane_ms = 0.0;
+    *n_pencil = *n_plane = 0;
+    for (auto& e : c->events) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e.a, e.b), "cudaEventElapsedTime");
+        if (e.kind == 0) { *pencil_ms += ms; (*n_pencil)++; }
+        else { *plane_ms += ms; (*n_plane)++; }
+    }
+    return MPC_OK;
+}
+
+int mpc_get_state(mpc_ctx* c, mpc_state* st) {
+    if (!c || !st) return fail(MPC_ERR_ARG, "null argument");
+    *st = c->state;
+    return MPC_OK;
+}
+int mpc_set_state(mpc_ctx* c, const mpc_state* st) {
+    if (!c || !st) return fail(MPC_ERR_ARG, "null argument");
+    c->state = *st;
+    return MPC_OK;
+}
+
+int mpc_field_upload(mpc_ctx* c, const double* A, int calibrate) {
+    if (!c || !A) return fail(MPC_ERR_ARG, "null argument");
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    double k = 1.0;
+    if (calibrate) {
+        if (!(c->p.Esig > 0)) return fail(MPC_ERR_ARG, "Esig must be positive to calibrate");
+        k = sqrt(c->p.puls_e / c->p.Esig);  // MPC.c:209 (A17: both parts)
+    }
+    PencilArgs a{};
+    a.in = c->io;
+    a.out = c->S;
+    a.in_scale = c->fs * k / (double)c->Nt;
+    rc = launch_pencil(c, mpc::PM_ENTRY_C128, a);
+    if (rc) return rc;
+    c->have_field = 1;
+    return MPC_OK;
+}
+
+// download the device field (complex128, physical units); optional per-pencil energies
+static int exit_to_io(mpc_ctx* c, int energies) {
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    PencilArgs a{};
+    a.in = c->S;
+    a.out = c->io;
+    a.out_scale = 1.0 / c->fs;
+    a.pencil_energy = energies ? c->penergy : nullptr;
+    return launch_pencil(c, mpc::PM_EXIT_C128, a);
+}
+
+int mpc_field_download(mpc_ctx* c, double* A) {
+    if (!c || !A) return fail(MPC_ERR_ARG, "null argument");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    int rc = exit_to_io(c, 0);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H field");
+    CK(cudaStreamSynchronize(c->st), "download");
+    return MPC_OK;
+}
+
+// one nonlinear step of the pencil sweep, in place on S
+static int pencil_step(mpc_ctx* c, double dz) {
+    PencilArgs a{};
+    a.in = c->S;
+    a.out = c->S;
+    a.nl = c->nl;
+    a.nl.dz = (float)dz;
+    return launch_pencil(c, mpc::PM_STEP, a);
+}
+
+static int bounces_between(double z0, double z1, double Cav) {
+    const double eps = 1e-9;
+    return (int)(floor(z1 / Cav + eps) - floor(z0 / Cav + eps));
+}
+
+int mpc_run_fixed(mpc_ctx* c, int nsteps) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    if (nsteps <= 0) return MPC_OK;
+    const double dz = c->state.dzz;
+    const double Cav = c->p.Cav;
+    const int lens = c->p.bounce_mode == MPC_BOUNCE_LENS;
+    const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
+    const long g0 = c->state.nstep;
+    auto sign_of = [&](long g) -> int { return lens ? 1 : pass_sign((double)g * dz + 1e-9 * Cav, Cav); };
+    auto bounce_after = [&](long g) -> int { return bounces_between((double)g * dz, (double)(g + 1) * dz, Cav); };
+    int rc;
+    TableSet t1, t2;
+    // first half step of step g0 on the normalised state
+    int s_prev = sign_of(g0);
+    if ((rc = get_tables(c, s_prev * dz / 2, dz / 2, sNP, &t1))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
+    for (int k = 0; k < nsteps; k++) {
+        const long g = g0 + k;
+        if ((rc = pencil_step(c, dz))) return rc;
+        const int nb = bounce_after(g);
+        const int last = (k == nsteps - 1);
+        const int s_next = sign_of(g + 1);
+        if (nb > 0) {
+            for (int b = 0; b < nb; b++) c->state.puls_e *= c->p.Ab_M;  // A24 fix
+        }
+        if (lens && nb > 0) {
+            if ((rc = get_tables(c, s_prev * dz / 2, dz / 2, sN, &t1))) return rc;
+            if (last) t2 = c->ident;
+            else if ((rc = get_tables(c, s_next * dz / 2, dz / 2, sNP, &t2))) return rc;
+            if ((rc = launch_plane(c, c->S, c->S, t1, &t2))) return rc;
+        } else if (last) {
+            if ((rc = get_tables(c, s_prev * dz / 2, dz / 2, sN, &t1))) return rc;
+            if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
+        } else {
+            if ((rc = get_tables(c, (s_prev + s_next) * dz / 2, dz, sN, &t1))) return rc;
+            if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
+        }
+        s_prev = s_next;
+    }
+    c->state.nstep += nsteps;
+    c->state.z = (double)c->state.nstep * dz;
+    c->state.signmem = sign_of(c->state.nstep);
+    return MPC_OK;
+}
+
+int mpc_ssfmprop(mpc_ctx* c, double* A, int sst_on, double dzz, int* signmem, double z, double* puls_e,
+                 double* BP1, double* BP2, double* y1, double* y2, double* bps1, double* bps2, int change) {
+    if (!c || !A || !signmem || !puls_e) return fail(MPC_ERR_ARG, "null argument");
+    if (change == 1 && (!BP1 || !BP2 || !y1 || !y2 || !bps1 || !bps2)) return fail(MPC_ERR_ARG, "null diagnostic output");
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    PencilArgs a{};
+    a.in = c->io;
+    a.out = c->S;
+    a.in_scale = c->fs / (double)c->Nt;
+    if ((rc = launch_pencil(c, mpc::PM_ENTRY_C128, a))) return rc;
+    // calcexpR's sign logic (propagation.c:377-382)
+    int signum = pass_sign(z, c->p.Cav);
+    if (-*signmem == signum) *signmem = -*signmem;
+    if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
+    const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
+    TableSet t1, t2;
+    if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sNP, &t1))) return rc;
+    if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sN, &t2))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
+    PencilArgs b{};
+    b.in = c->S;
+    b.out = c->S;
+    b.nl = c->nl;
+    b.nl.dz = (float)dzz;
+    b.nl.sst_c = (sst_on == 1) ? c->sst_c_full : 0.0f;
+    if ((rc = launch_pencil(c, mpc::PM_STEP, b))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t2, nullptr))) return rc;
+    c->have_field = 1;
+    if ((rc = exit_to_io(c, change == 1))) return rc;
+    CK(cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H field");
+    if (change == 1) {
+        // propagation.c:334-341, as written (after calcexpR the condition cannot hold)
+        const int s2 = pass_sign(z, c->p.Cav);
+        if (*signmem == -s2) {
+            *puls_e = *puls_e * c->p.Ab_M;
+            *signmem *= -1;
+        }
+        k_beam_profiles<<<(c->Nx + 255) / 256, 256, 0, c->st>>>(c->penergy, c->Nx, c->Ny, c->dred, c->dred + c->Nx);
+        CK(cudaGetLastError(), "k_beam_profiles");
+        CK(cudaMemcpyAsync(BP1, c->dred, sizeof(double) * c->Nx, cudaMemcpyDeviceToHost, c->st), "D2H BP1");
+        CK(cudaMemcpyAsync(BP2, c->dred + c->Nx, sizeof(double) * c->Ny, cudaMemcpyDeviceToHost, c->st), "D2H BP2");
+    }
+    CK(cudaStreamSynchronize(c->st), "ssfmprop");
+    if (change == 1) {
+        mpc_calc1oes(BP1, c->Nx, c->r.data(), bps1, y1);
+        mpc_calc1oes(BP2, c->Ny, c->r.data(), bps2, y2);
+    }
+    return MPC_OK;
+}
+
+// 1/e^2 radius search (propagation.c:460-504), serial meaning of its parallel loops.
+int mpc_calc1oes(const double* BP, int n, const double* r, double* vald, double* y) {
+    double bpex = 0;
+    int posi1 = 0, posi2 = 0;
+    for (int k = 0; k < n; k++)
+        if (BP[k] > bpex) bpex = BP[k];
+    const double lvl = 1.0 / pow(exp(1.0), 2.0);
+    double best = 0;
+    for (int k = 0; k < n / 2; k++) {
+        const double h = fabs(BP[k] / bpex - lvl);
+        if (k == 0) best = h;
+        else if (h < best) { best = h; posi1 = k; }
+    }
+    for (int k = n / 2; k < n; k++) {
+        const double h = fabs(BP[k] / bpex - lvl);
+        if (k == n / 2) best = h;
+        else if (h < best) { best = h; posi2 = k; }
+    }
+    *vald = -r[posi1] + r[posi2];
+    y[0] = r[posi1];
+    y[1] = r[posi2];
+    y[2] = BP[posi1];
+    y[3] = BP[posi2];
+    return MPC_OK;
+}
+
+int mpc_linearstep(mpc_ctx* c, double* A, const double* exp_D0, const double* expR) {
+    if (!c || !A || !exp_D0 || !expR) return fail(MPC_ERR_ARG, "null argument");
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    // caller tables -> position order, conj(expR) along x and y, D scaled by 1/(Nx Ny)
+    const int Nx = c->Nx, Ny = c->Ny, Nt = c->Nt;
+    std::vector<float2> h(Nx + Ny + Nt);
+    for (int i = 0; i < Nx; i++) {
+        const int f = c->hfx[i];
+        h[i] = make_float2((float)expR[2 * f], (float)-expR[2 * f + 1]);
+    }
+    for (int j = 0; j < Ny; j++) {
+        const int f = c->hfy[j];
+        h[Nx + j] = make_float2((float)expR[2 * f], (float)-expR[2 * f + 1]);
+    }
+    const double sc = 1.0 / (double)c->NP;
+    for (int k = 0; k < Nt; k++) {
+        const int f = c->hft[k];
+        h[Nx + Ny + k] = make_float2((float)(exp_D0[2 * f] * sc), (float)(exp_D0[2 * f + 1] * sc));
+    }
+    float2* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(float2) * h.size()), "cudaMalloc caller tables");
+    cudaError_t e = cudaMemcpyAsync(buf, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice, c->st);
+    TableSet t{buf, buf + Nx, buf + Nx + Ny};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return fail(MPC_ERR_CUDA, "H2D linearstep", e);
+    }
+    PencilArgs a{};
+    a.in = c->io;
+    a.out = c->S;
+    a.in_scale = c->fs / (double)Nt;
+    rc = launch_pencil(c, mpc::PM_ENTRY_C128, a);
+    if (!rc) rc = launch_plane(c, c->S, c->S, t, nullptr);
+    if (!rc) rc = exit_to_io(c, 0);
+    if (!rc) {
+        e = cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        if (e != cudaSuccess) rc = fail(MPC_ERR_CUDA, "linearstep", e);
+    }
+    cudaStreamSynchronize(c->st);
+    cudaFree(buf);
+    c->have_field = 1;
+    return rc;
+}
+
+int mpc_calcexpR(mpc_ctx* c, double* expR, int* signmem, double z, double dzz) {
+    if (!c || !expR || !signmem) return fail(MPC_ERR_ARG, "null argument");
+    int signum = pass_sign(z, c->p.Cav);
+    if (-*signmem == signum) *signmem = -*signmem;
+    if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
+    TableSet t;
+    int rc = get_tables(c, signum * dzz, 0.0, 1.0, &t);
+    if (rc) return rc;
+    std::vector<float2> h(c->Nx);
+    CK(cudaMemcpyAsync(h.data(), t.Rx, sizeof(float2) * c->Nx, cudaMemcpyDeviceToHost, c->st), "D2H table");
+    CK(cudaStreamSynchronize(c->st), "calcexpR");
+    // the device table is conj(expR) in position order; the reference returns expR in FFT order
+    for (int px = 0; px < c->Nx; px++) {
+        const int f = c->hfx[px];
+        expR[2 * f] = h[px].x;
+        expR[2 * f + 1] = -h[px].y;
+    }
+    return MPC_OK;
+}
+
+int mpc_ioniz(mpc_ctx* c, const double* A, double* tau_c, double* fe_sp) {
+    if (!c || !A || !tau_c || !fe_sp) return fail(MPC_ERR_ARG, "null argument");
+    if (!c->ion_gas_ok) return fail(MPC_ERR_ARG, "unknown gas");
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    if ((rc = ensure_io(c, 1))) return rc;
+    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    PencilArgs a{};
+    a.in = c->io;
+    a.in_scale = c->fs;
+    a.nl = c->nl;
+    a.nl.plasma = 1;
+    double* tau_d = reinterpret_cast<double*>(c->io2);
+    double* fe_d = tau_d + c->N;
+    a.tau_out = tau_d;
+    a.fe_out = fe_d;
+    if ((rc = launch_pencil(c, mpc::PM_IONIZ, a))) return rc;
+    CK(cudaMemcpyAsync(tau_c, tau_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H tau_c");
+    CK(cudaMemcpyAsync(fe_sp, fe_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H fe_sp");
+    CK(cudaStreamSynchronize(c->st), "ioniz");
+    return MPC_OK;
+}
+
+int mpc_ADK(mpc_ctx* c, long n, const double* E, double* r1, double* r2) {
+    if (!c || !E || !r1 || !r2 || n < 0) return fail(MPC_ERR_ARG, "null argument");
+    if (n == 0) return MPC_OK;
+    double* d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double) * 3 * n), "cudaMalloc ADK");
+    cudaError_t e = cudaMemcpyAsync(d, E, sizeof(double) * n, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) {
+        k_adk<<<(int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, c->st>>>(n, d, d + n, d + 2 * n, c->adk);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r1, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r2, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(MPC_ERR_CUDA, "ADK", e);
+    return MPC_OK;
+}
+
+// the dz rule of setStep (propagation.c:636-676) given err
+static void step_rule(double err, double* dzz, double def_err, double dzmin, const double* y1, const double* y2, int* bad) {
+    const double err_fact = pow(2.0, 1.0 / 3.0);
+    *bad = 0;
+    if (err > 2.0 * def_err) {
+        const double u = *dzz / 2.0;
+        if (u > dzmin) {
+            *dzz = u;
+            *bad = 1;
+        }
+    } else if (err > def_err && err < 2.0 * def_err) {
+        const double u = *dzz / err_fact;
+        if (u > dzmin) *dzz = u;
+    } else if (err > 0.5 * def_err && err <= def_err) {
+    } else {
+        const double u = *dzz * err_fact;
+        if (!(u > 100 * (y2[1] + y1[1]) / 2.0)) *dzz = u;
+    }
+}
+
+int mpc_setStep(mpc_ctx* c, double* dzz, const double* C1, const double* C2, const double* y1, const double* y2,
+                int* bad, double* err) {
+    if (!c || !dzz || !C1 || !C2 || !y1 || !y2 || !bad || !err) return fail(MPC_ERR_ARG, "null argument");
+    int rc = ensure_io(c, 0);
+    if (rc) return rc;
+    if ((rc = ensure_io(c, 1))) return rc;
+    CK(cudaMemcpyAsync(c->io, C1, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D C1");
+    CK(cudaMemcpyAsync(c->io2, C2, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D C2");
+    CK(cudaMemsetAsync(c->dred, 0, 2 * sizeof(double), c->st), "memset");
+    k_diffnorm_c128<<<c->nsm * 4, 256, 0, c->st>>>(c->io, c->io2, c->N, c->dred);
+    CK(cudaGetLastError(), "k_diffnorm_c128");
+    double s[2];
+    CK(cudaMemcpyAsync(s, c->dred, sizeof s, cudaMemcpyDeviceToHost, c->st), "D2H sums");
+    CK(cudaStreamSynchronize(c->st), "setStep");
+    *err = sqrt(s[0]) / sqrt(s[1]);
+    step_rule(*err, dzz, c->p.def_err, c->p.dzmin, y1, y2, bad);
+    return MPC_OK;
+}
+
+int mpc_diag(mpc_ctx* c, double* temp, double* spec, double* BP1, double* BP2) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    const int Nt = c->Nt;
+    double* dtemp = c->dred;
+    double* dspec = c->dred + Nt;
+    int rc;
+    const double phys2 = 1.0 / (c->fs * c->fs);
+    if (temp) {
+        CK(cudaMemsetAsync(dtemp, 0, sizeof(double) * Nt, c->st), "memset temp");
+        PencilArgs a{};
+        a.in = c->S;
+        a.temp = dtemp;
+        a.out_scale = 1.0 / c->fs;
+        if ((rc = launch_pencil(c, mpc::PM_TEMP, a))) return rc;
+        CK(cudaMemcpyAsync(temp, dtemp, sizeof(double) * Nt, cudaMemcpyDeviceToHost, c->st), "D2H temp");
+        CK(cudaStreamSynchronize(c->st), "temp");
+    }
+    if (spec) {
+        // S = FFT_t(a)/Nt  ->  |FFT_t A|^2 = Nt^2 |S|^2 / fs^2
+        k_spec<<<Nt, 256, 0, c->st>>>(c->S, (int)c->NP, c->ops->SLO, c->dft, (double)Nt * Nt * phys2, dspec);
+        CK(cudaGetLastError(), "k_spec");
+        CK(cudaMemcpyAsync(spec, dspec, sizeof(double) * Nt, cudaMemcpyDeviceToHost, c->st), "D2H spec");
+        CK(cudaStreamSynchronize(c->st), "spec");
+    }
+    if (BP1 || BP2) {
+        if ((rc = exit_to_io(c, 1))) return rc;
+        double* d1 = c->dred;
+        double* d2 = c->dred + c->Nx;
+        k_beam_profiles<<<(c->Nx + 255) / 256, 256, 0, c->st>>>(c->penergy, c->Nx, c->Ny, d1, d2);
+        CK(cudaGetLastError(), "k_beam_profiles");
+        if (BP1) CK(cudaMemcpyAsync(BP1, d1, sizeof(double) * c->Nx, cudaMemcpyDeviceToHost, c->st), "D2H BP1");
+        if (BP2) CK(cudaMemcpyAsync(BP2, d2, sizeof(double) * c->Ny, cudaMemcpyDeviceToHost, c->st), "D2H BP2");
+        CK(cudaStreamSynchronize(c->st), "beam profiles");
+    }
+    return MPC_OK;
+}
+
+int mpc_energy(mpc_ctx* c, double* energy) {
+    if (!c || !energy) return fail(MPC_ERR_ARG, "null argument");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    CK(cudaMemsetAsync(c->dred, 0, sizeof(double), c->st), "memset");
+    k_norm2_c64<<<c->nsm * 4, 256, 0, c->st>>>(c->S, c->N, c->dred);
+    CK(cudaGetLastError(), "k_norm2_c64");
+    double s = 0;
+    CK(cudaMemcpyAsync(&s, c->dred, sizeof s, cudaMemcpyDeviceToHost, c->st), "D2H energy");
+    CK(cudaStreamSynchronize(c->st), "energy");
+    // sum_t |a|^2 = Nt sum_omega |S|^2 ;  |A|^2 = |a|^2 / fs^2
+    *energy = s * (double)c->Nt / (c->fs * c->fs) * c->p.dr * c->p.dr * c->p.deltat * HBAR * c->p.w0;
+    return MPC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,215 @@
+// mpc_fft.cuh -- complex64 arithmetic and in-shared-memory FFT stages for sm_103a.
+//
+// The propagator's transforms (t pencils, x rows, y columns) are all batched power-of-two
+// FFTs done in shared memory: a forward transform is an in-place decimation-in-frequency
+// (DIF) sweep that leaves the spectrum in digit-reversed "position" order, an inverse is the
+// exact transpose sweep (decimation in time, DIT) that takes position order back to natural
+// order.  Nothing between a forward and an inverse transform needs natural frequency order,
+// so no reordering pass ever runs; diagonal operators (dispersion, diffraction, -i*omega) are
+// indexed through a position -> frequency table built on the host (mpc_freq_of_pos).
+//
+// Radix plan of a length-L stage: 16 while L >= 16, else L (so 2048 = 16*16*8,
+// 1024 = 16*16*4, 512 = 16*16*2, 256 = 16*16, 128 = 16*8, 64 = 16*4).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mpc {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by -i (forward kernel sign) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+// multiply by exp(-+i*pi/4) = (1 -+ i)/sqrt(2)
+template <bool INV>
+__device__ __forceinline__ float2 mul_w8(float2 a) {
+    const float h = 0.70710678118654752f;
+    return INV ? make_float2((a.x - a.y) * h, (a.x + a.y) * h)
+               : make_float2((a.x + a.y) * h, (a.y - a.x) * h);
+}
+// multiply by exp(-+3i*pi/4) = (-1 -+ i)/sqrt(2)
+template <bool INV>
+__device__ __forceinline__ float2 mul_w83(float2 a) {
+    const float h = 0.70710678118654752f;
+    return INV ? make_float2((-a.x - a.y) * h, (a.x - a.y) * h)
+               : make_float2((a.y - a.x) * h, (-a.x - a.y) * h);
+}
+
+// ---- small DFTs in registers, natural order in and out, unnormalised ------------------
+template <bool INV>
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
+    const float2 s02 = cadd(x0, x2), d02 = csub(x0, x2);
+    const float2 s13 = cadd(x1, x3), d13 = mul_mi<INV>(csub(x1, x3));
+    x0 = cadd(s02, s13);
+    x2 = csub(s02, s13);
+    x1 = cadd(d02, d13);
+    x3 = csub(d02, d13);
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 (&v)[R]);
+
+template <>
+__device__ __forceinline__ void dft<2, false>(float2 (&v)[2]) { dft2<false>(v[0], v[1]); }
+template <>
+__device__ __forceinline__ void dft<2, true>(float2 (&v)[2]) { dft2<true>(v[0], v[1]); }
+template <>
+__device__ __forceinline__ void dft<4, false>(float2 (&v)[4]) { dft4<false>(v[0], v[1], v[2], v[3]); }
+template <>
+__device__ __forceinline__ void dft<4, true>(float2 (&v)[4]) { dft4<true>(v[0], v[1], v[2], v[3]); }
+
+// 8 = 4 x 2: n = 2 n1 + n2, k = k1 + 4 k2
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 (&v)[8]) {
+    dft4<INV>(v[0], v[2], v[4], v[6]);   // Y[0][k1] at v[0],v[2],v[4],v[6]
+    dft4<INV>(v[1], v[3], v[5], v[7]);   // Y[1][k1] at v[1],v[3],v[5],v[7]
+    v[3] = mul_w8<INV>(v[3]);
+    v[5] = mul_mi<INV>(v[5]);
+    v[7] = mul_w83<INV>(v[7]);
+    float2 o[8];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+        o[k1] = cadd(v[2 * k1], v[2 * k1 + 1]);
+        o[k1 + 4] = csub(v[2 * k1], v[2 * k1 + 1]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = o[i];
+}
+template <>
+__device__ __forceinline__ void dft<8, false>(float2 (&v)[8]) { dft8<false>(v); }
+template <>
+__device__ __forceinline__ void dft<8, true>(float2 (&v)[8]) { dft8<true>(v); }
+
+// 16 = 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2, inner twiddle W16^(n2 k1)
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) dft4<INV>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+    // now v[n2 + 4 k1] = Y[n2][k1]
+    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f;
+    const float sg = INV ? 1.0f : -1.0f;
+    const float2 w1 = make_float2(c1, sg * s1);   // W16^1
+    const float2 w3 = make_float2(s1, sg * c1);   // W16^3
+    const float2 w9 = make_float2(-c1, -sg * s1); // W16^9
+    v[5] = cmul(v[5], w1);            // n2=1,k1=1
+    v[9] = mul_w8<INV>(v[9]);         // n2=1,k1=2 : W16^2
+    v[13] = cmul(v[13], w3);          // n2=1,k1=3
+    v[6] = mul_w8<INV>(v[6]);         // n2=2,k1=1 : W16^2
+    v[10] = mul_mi<INV>(v[10]);       // n2=2,k1=2 : W16^4
+    v[14] = mul_w83<INV>(v[14]);      // n2=2,k1=3 : W16^6
+    v[7] = cmul(v[7], w3);            // n2=3,k1=1
+    v[11] = mul_w83<INV>(v[11]);      // n2=3,k1=2 : W16^6
+    v[15] = cmul(v[15], w9);          // n2=3,k1=3
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // now v[4 k1 + k2] = X[k1 + 4 k2]; transpose to natural order
+    float2 o[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++) o[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = o[i];
+}
+template <>
+__device__ __forceinline__ void dft<16, false>(float2 (&v)[16]) { dft16<false>(v); }
+template <>
+__device__ __forceinline__ void dft<16, true>(float2 (&v)[16]) { dft16<true>(v); }
+
+template <int L>
+struct Radix {
+    static constexpr int R = (L >= 16) ? 16 : L;
+};
+
+// ---- batched in-place stages over a shared-memory view --------------------------------
+// View: NLINES independent lines of length N; element `pos` of line `l` lives at
+// V::at(pos, l).  Work items are (line, butterfly) pairs, lines fastest across threads.
+// tw: W_N^k = exp(-2 pi i k / N), k < N, complex64 rounded from FP64.
+//
+// DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
+template <int N, int L, class V>
+__device__ __forceinline__ void dif_stage(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+    constexpr int R = Radix<L>::R;
+    constexpr int S = L / R;
+    constexpr int NB = N / R;
+    constexpr int TOT = NB * V::NLINES;
+    for (int idx = tid; idx < TOT; idx += nthr) {
+        const int line = idx % V::NLINES;
+        const int g = idx / V::NLINES;
+        const int b = g / S, j = g - (g / S) * S;
+        const int base = b * L + j;
+        float2 v[R];
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = s[V::at(base + S * q, line)];
+        dft<R, false>(v);
+        if (S > 1) {
+#pragma unroll
+            for (int k = 1; k < R; k++) v[k] = cmul(v[k], __ldg(&tw[j * k * (N / L)]));
+        }
+#pragma unroll
+        for (int q = 0; q < R; q++) s[V::at(base + S * q, line)] = v[q];
+    }
+}
+
+// DIT stage (exact transpose of the DIF stage with conjugate twiddles).
+template <int N, int L, class V>
+__device__ __forceinline__ void dit_stage(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+    constexpr int R = Radix<L>::R;
+    constexpr int S = L / R;
+    constexpr int NB = N / R;
+    constexpr int TOT = NB * V::NLINES;
+    for (int idx = tid; idx < TOT; idx += nthr) {
+        const int line = idx % V::NLINES;
+        const int g = idx / V::NLINES;
+        const int b = g / S, j = g - (g / S) * S;
+        const int base = b * L + j;
+        float2 v[R];
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = s[V::at(base + S * q, line)];
+        if (S > 1) {
+#pragma unroll
+            for (int k = 1; k < R; k++) v[k] = cmulc(v[k], __ldg(&tw[j * k * (N / L)]));
+        }
+        dft<R, true>(v);
+#pragma unroll
+        for (int q = 0; q < R; q++) s[V::at(base + S * q, line)] = v[q];
+    }
+}
+
+// Whole forward transform (natural -> position order).  Ends with a __syncthreads.
+template <int N, int L, class V>
+__device__ __forceinline__ void dif_all(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+    dif_stage<N, L, V>(s, tw, tid, nthr);
+    __syncthreads();
+    constexpr int R = Radix<L>::R;
+    if constexpr (L / R > 1) dif_all<N, L / R, V>(s, tw, tid, nthr);
+}
+
+// Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
+template <int N, int L, class V>
+__device__ __forceinline__ void dit_all(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+    constexpr int R = Radix<L>::R;
+    if constexpr (L / R > 1) dit_all<N, L / R, V>(s, tw, tid, nthr);
+    dit_stage<N, L, V>(s, tw, tid, nthr);
+    __syncthreads();
+}
+
+}  // namespace mpc

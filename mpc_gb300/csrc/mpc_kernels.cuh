@@ -1,0 +1,695 @@
+// mpc_kernels.cuh -- the split-step propagator's two HBM sweeps and their helpers.
+//
+// Device layout of the field between sweeps ("slot layout"): the field is kept in the
+// (x, y, omega) domain, omega in FFT position order.  Slots are interleaved in groups of
+// SLO: element (slot s, pencil q = y*Nx + x) lives at ((s/SLO)*Nx*Ny + q)*SLO + s%SLO.
+// SLO is 2 for Nt = 2048 (8 pencils per tile -> 8*2*8 B = 128 B contiguous per row) and 1
+// for Nt <= 1024 (>= 16 pencils per tile), so every t-row a pencil tile reads is >= 128 B:
+// strided 64 B rows reach only 60% of HBM bandwidth on GB300, 128 B rows 94%.
+//
+// Sweep 1, pencil pass (one CTA per tile of P neighbouring (x,y) pencils, all of t):
+//   IFFT_t of -i*omega*S -> dA,  IFFT_t of S -> A,  nonlinear step N(dz) (Kerr, self-
+//   steepening, ADK ionization with two affine prefix scans along t, plasma absorption and
+//   defocusing, A *= exp(dz*A_nl)),  FFT_t -> S.
+// Sweep 2, plane pass (one thread-block cluster per SLO omega-planes):
+//   FFT_x, FFT_y, multiply by Rx(kx) Ry(ky) D(omega) / (Nx Ny Nt), IFFT_y, IFFT_x; rows
+//   and columns move between the cluster's CTAs through distributed shared memory.
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpc_fft.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace mpc {
+
+constexpr int kThreads = 512;          // both sweeps
+constexpr int kTilePoints = 16384;     // pencil tile: P * Nt complex points (128 KB)
+
+// FP32 constants of the nonlinear step, computed on the host in FP64.
+struct NLConst {
+    float dz;        // step length [m]
+    float gam;       // gamma2 / fs^2: Kerr phase per unit |a|^2 [1/m]
+    float sst_c;     // gamma2 / (w0 fs^2), 0 when self-steepening is off
+    float I_scale;   // intensity [W/m^2] per unit |a|^2
+    float E_c;       // field in atomic units = sqrt(I) * E_c
+    float lnK1[2], K3[2], lnK3[2], K5[2];   // ADK constants of the two ionization stages
+    float Kon;       // deltat / T0
+    float ve_c;      // drift velocity = F * ve_c
+    float K3c;       // sigma_coll * rho_nt
+    float K4w0;      // k0 w0^2 / (n0 rho_c)
+    float w0sq;      // w0^2
+    float inv_w0;    // 1 / w0
+    float inv_I1;    // 1 / I1 (I1 in eV, as the reference divides by it)
+    float rho_half;  // rho_nt / 2
+    int plasma;      // 1 = ionization and plasma terms on
+};
+
+// Pencil tile view: line = pencil p, element (pos, p).  For P < 16 a pad keeps the
+// span-1 FFT stages and the per-thread t walks free of shared-memory bank conflicts.
+template <int NT, int P>
+struct PencilView {
+    static constexpr int NLINES = P;
+    static __device__ __forceinline__ int at(int pos, int p) {
+        if constexpr (P < 16) return pos * P + p + P * ((pos >> 4) + (pos >> 5));
+        else return pos * P + p;
+    }
+    static constexpr int SIZE = (P < 16) ? (NT * P + P * (NT / 16 + NT / 32)) : NT * P;
+};
+
+enum PencilMode : int {
+    PM_ENTRY_C128 = 0,  // real-space complex128 (reference layout, physical units) -> S
+    PM_ENTRY_C64 = 1,   // real-space complex64 (reference layout, device units) -> S
+    PM_STEP = 2,        // S -> N(dz) -> S
+    PM_EXIT_C128 = 3,   // S -> real-space complex128 (physical units) + per-pencil energy
+    PM_EXIT_C64 = 4,    // S -> real-space complex64 (device units) + per-pencil energy
+    PM_TEMP = 5,        // S -> temporal profile sums only (no store)
+    PM_IONIZ = 6,       // real-space complex128 -> tau_c, freeelectrons_sp (FP64, reference layout)
+};
+
+struct PencilArgs {
+    const void* in;          // input field (layout by mode)
+    void* out;               // output field (may alias in)
+    float2* scratch;         // per-CTA dA scratch, gridDim.x * Nt * P complex64
+    const float2* tw;        // W_Nt table
+    const float* wpos;       // omega of each t position (FFT position order), Nt
+    double* pencil_energy;   // EXIT: sum_t |out|^2 per pencil, Nx*Ny
+    double* temp;            // TEMP: sum_xy |out|^2 per t, Nt (accumulated)
+    double* tau_out;         // IONIZ: tau_c, reference layout
+    double* fe_out;          // IONIZ: freeelectrons_sp, reference layout
+    double in_scale;         // ENTRY: input multiplier (to device units, includes 1/Nt)
+    double out_scale;        // EXIT/TEMP: output multiplier (from device units)
+    int NP;                  // Nx * Ny
+    int ntiles;              // NP / P
+    NLConst nl;
+};
+
+__device__ __forceinline__ size_t slot_index(int s, int q, int NP, int SLO) {
+    return ((size_t)(s / SLO) * NP + q) * SLO + (s % SLO);
+}
+
+// ---------------------------------------------------------------------------------------
+// Affine-map scans of the ionization prefix (plasma.c:223-231, run forward in t).
+//   R_k = (1 - b_k)(R_{k-1} + a_k) + b_k          map (B, C): R -> (1-B) R + C
+//   (u, v)_{k+1} = (u_k + c2_k v_k, g_k - u_k)     map (M, o): x -> M x + o
+// with a_k = W1 Kon, b_k = Wava Kon, c2_k = W2 Kon, g_k = 1 - exp(-R_k); u = ions2,
+// v = ions1, both zero before the first slice; fe_sp[k] = (v_k + 2 u_k) sigma_k.
+// Chunk maps are composed in FP32 inside a thread's 32 points and across chunks in FP64.
+// ---------------------------------------------------------------------------------------
+struct MapR { double B, C; };
+struct MapUV { double m00, m01, m10, m11, o0, o1; };
+
+__device__ __forceinline__ MapR compose(const MapR& first, const MapR& then) {
+    MapR r;
+    r.B = first.B + then.B - first.B * then.B;
+    r.C = (1.0 - then.B) * first.C + then.C;
+    return r;
+}
+__device__ __forceinline__ MapUV compose(const MapUV& f, const MapUV& t) {
+    MapUV r;
+    r.m00 = t.m00 * f.m00 + t.m01 * f.m10;
+    r.m01 = t.m00 * f.m01 + t.m01 * f.m11;
+    r.m10 = t.m10 * f.m00 + t.m11 * f.m10;
+    r.m11 = t.m10 * f.m01 + t.m11 * f.m11;
+    r.o0 = t.m00 * f.o0 + t.m01 * f.o1 + t.o0;
+    r.o1 = t.m10 * f.o0 + t.m11 * f.o1 + t.o1;
+    return r;
+}
+template <class M>
+__device__ __forceinline__ M map_ident();
+template <>
+__device__ __forceinline__ MapR map_ident<MapR>() { return MapR{0.0, 0.0}; }
+template <>
+__device__ __forceinline__ MapUV map_ident<MapUV>() { return MapUV{1.0, 0.0, 0.0, 1.0, 0.0, 0.0}; }
+
+template <class M>
+__device__ __forceinline__ M shfl_up_map(const M& m, int off) {
+    M r;
+    double* dst = reinterpret_cast<double*>(&r);
+    const double* src = reinterpret_cast<const double*>(&m);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(M) / sizeof(double)); i++) dst[i] = __shfl_up_sync(0xffffffffu, src[i], off);
+    return r;
+}
+
+// Exclusive scan over the TPP chunk maps of each of P pencils, in place in `maps`
+// (index p * TPP + c).  One warp per pencil; each lane composes TPP/32 (or 1) chunks.
+template <class M, int P, int TPP>
+__device__ __forceinline__ void scan_chunks(M* maps, int tid) {
+    const int warp = tid >> 5, lane = tid & 31;
+    constexpr int NW = kThreads / 32;
+    constexpr int CPL = (TPP + 31) / 32;
+    for (int p = warp; p < P; p += NW) {
+        M* row = maps + p * TPP;
+        M acc = map_ident<M>();
+        const int c0 = lane * CPL;
+#pragma unroll
+        for (int j = 0; j < CPL; j++)
+            if (c0 + j < TPP) acc = compose(acc, row[c0 + j]);
+        // inclusive warp scan of lane aggregates
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const M prev = shfl_up_map(acc, off);
+            if (lane >= off) acc = compose(prev, acc);
+        }
+        M excl = shfl_up_map(acc, 1);
+        if (lane == 0) excl = map_ident<M>();
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < CPL; j++) {
+            if (c0 + j < TPP) {
+                const M own = row[c0 + j];
+                row[c0 + j] = excl;
+                excl = compose(excl, own);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Per-point ionization inputs of one sample (plasma.c:133-213 in FP32, the A18 fix applied).
+struct IonPoint {
+    float a, b, c2;  // scan coefficients
+    float qw;        // K4 w0 / (u^2 + w0^2) = sigma * w0 * tau_c (defocusing weight)
+    float sigma;     // K4 tau_c / (1 + w0^2 tau_c^2), tau_c = 1/u
+    float u;         // 1 / tau_c = sigma_coll rho_nt v_e
+    float I;
+};
+__device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
+    IonPoint r;
+    float I = (a.x * a.x + a.y * a.y) * c.I_scale;
+    if (I == 0.0f) I = 1e-30f;
+    const float F = sqrtf(I) * c.E_c;
+    const float lnF = logf(F);
+    const float invF = 1.0f / F;
+    float w[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const float ex = c.K3[s] * invF * (1.0f / 3.0f);
+        w[s] = (ex < 100.0f) ? expf(c.lnK1[s] + c.K5[s] * (c.lnK3[s] - lnF) - ex) : 0.0f;
+    }
+    const float u = c.K3c * (F * c.ve_c);      // 1 / tau_c
+    const float qw = c.K4w0 / fmaf(u, u, c.w0sq);
+    const float sigma = qw * u * c.inv_w0;
+    const float wava = sigma * I * c.inv_I1;
+    r.a = w[0] * c.Kon;
+    r.b = wava * c.Kon;
+    r.c2 = w[1] * c.Kon;
+    r.qw = qw;
+    r.sigma = sigma;
+    r.u = u;
+    r.I = I;
+    return r;
+}
+
+// Nonlinear step on a tile holding A(t) of P pencils in shared memory (natural t order).
+// IONIZ_ONLY = false: A *= exp(dz * A_nl) in place (propagation.c:244-327 with the A13/A14
+// fixes).  IONIZ_ONLY = true: write tau_c and freeelectrons_sp (plasma.c:118-245 outputs)
+// in the reference layout instead, A untouched.
+template <int NT, int P, bool IONIZ_ONLY>
+__device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restrict__ scr, const NLConst& c,
+                                               void* scan_mem, int tid, double* tau_out, double* fe_out,
+                                               int q0, int NP) {
+    using V = PencilView<NT, P>;
+    constexpr int TPP = NT / 32;
+    const int p = tid % P;
+    const int ch = tid / P;       // chunk index within the pencil
+    const int t0 = ch * 32;
+    if (c.plasma) {
+        MapR* mr = reinterpret_cast<MapR*>(scan_mem);
+        MapUV* muv = reinterpret_cast<MapUV*>(scan_mem);
+        // S1: chunk maps of the R recurrence
+        {
+            float B = 0.0f, C = 0.0f;
+            for (int i = 0; i < 32; i++) {
+                const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
+                const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
+                C = fmaf(1.0f - ip.b, C, Ck);
+                B = B + ip.b - B * ip.b;
+            }
+            mr[p * TPP + ch] = MapR{(double)B, (double)C};
+        }
+        __syncthreads();
+        scan_chunks<MapR, P, TPP>(mr, tid);
+        __syncthreads();
+        const float Rin = (float)mr[p * TPP + ch].C;
+        __syncthreads();
+        // S2: chunk maps of the (ions2, ions1) recurrence
+        {
+            float R = Rin;
+            float m00 = 1.f, m01 = 0.f, m10 = 0.f, m11 = 1.f, o0 = 0.f, o1 = 0.f;
+            for (int i = 0; i < 32; i++) {
+                const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
+                R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
+                const float g = -expm1f(-R);
+                const float n00 = fmaf(ip.c2, m10, m00), n01 = fmaf(ip.c2, m11, m01);
+                const float no0 = fmaf(ip.c2, o1, o0), no1 = g - o0;
+                m10 = -m00; m11 = -m01; m00 = n00; m01 = n01;
+                o1 = no1; o0 = no0;
+            }
+            muv[p * TPP + ch] = MapUV{m00, m01, m10, m11, o0, o1};
+        }
+        __syncthreads();
+        scan_chunks<MapUV, P, TPP>(muv, tid);
+        __syncthreads();
+        float u = (float)muv[p * TPP + ch].o0;
+        float v = (float)muv[p * TPP + ch].o1;
+        __syncthreads();
+        // S3: apply the nonlinear step
+        float R = Rin;
+        for (int i = 0; i < 32; i++) {
+            const int t = t0 + i;
+            const float2 a = s[V::at(t, p)];
+            const IonPoint ip = ion_point(a, c);
+            R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
+            const float g = -expm1f(-R);
+            const float ions = fmaf(2.0f, u, v);
+            if constexpr (IONIZ_ONLY) {
+                const size_t gi = (size_t)t * NP + q0 + p;
+                tau_out[gi] = 1.0 / (double)ip.u;
+                fe_out[gi] = (double)ions * (double)ip.sigma;
+                const float nu = fmaf(ip.c2, v, u);
+                v = g - u;
+                u = nu;
+                continue;
+            }
+            const float pl = c.rho_half * ions;
+            float re = -pl * ip.sigma;
+            float im = c.gam * (a.x * a.x + a.y * a.y) - pl * ip.qw;
+            if (c.sst_c != 0.0f) {
+                const float2 d = scr[t * P + p];
+                const float2 sd = cmulc(d, a);  // d * conj(a)
+                re = fmaf(-3.0f * c.sst_c, sd.x, re);
+                im = fmaf(-c.sst_c, sd.y, im);
+            }
+            const float nu = fmaf(ip.c2, v, u);
+            v = g - u;
+            u = nu;
+            const float amp = expf(c.dz * re);
+            float sn, cs;
+            sincosf(c.dz * im, &sn, &cs);
+            s[V::at(t, p)] = cmul(a, make_float2(amp * cs, amp * sn));
+        }
+    } else {
+        for (int i = 0; i < 32; i++) {
+            const int t = t0 + i;
+            const float2 a = s[V::at(t, p)];
+            float re = 0.0f;
+            float im = c.gam * (a.x * a.x + a.y * a.y);
+            if (c.sst_c != 0.0f) {
+                const float2 d = scr[t * P + p];
+                const float2 sd = cmulc(d, a);
+                re = -3.0f * c.sst_c * sd.x;
+                im = fmaf(-c.sst_c, sd.y, im);
+            }
+            const float amp = expf(c.dz * re);
+            float sn, cs;
+            sincosf(c.dz * im, &sn, &cs);
+            s[V::at(t, p)] = cmul(a, make_float2(amp * cs, amp * sn));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pencil pass
+// ---------------------------------------------------------------------------------------
+template <int NT, int P, int SLO>
+struct PencilCfg {
+    using View = PencilView<NT, P>;
+    static constexpr int TPP = NT / 32;                 // 32-point chunks per pencil
+    static constexpr int SMEM_FIELD = View::SIZE * 8;  // bytes
+    static constexpr int SMEM_SCAN = P * TPP * (int)sizeof(MapUV);
+    static constexpr int SMEM_TEMP = NT * 8;            // FP64 temporal sums (TEMP mode)
+    static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TEMP;
+    static_assert(NT * P == kTilePoints, "tile must hold 16384 points");
+    static_assert((P * SLO) % 2 == 0, "rows must be whole float4s");
+};
+
+// load a slot-layout tile into shared memory, optionally multiplied by -i*omega(pos)
+template <int NT, int P, int SLO, bool DERIV>
+__device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ g, const float* __restrict__ wpos,
+                                          int q0, int NP, int tid) {
+    using V = PencilView<NT, P>;
+    constexpr int F4_PER_ROW = P * SLO / 2;
+    constexpr int ROWS = NT / SLO;
+    const float4* g4 = reinterpret_cast<const float4*>(g);
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += kThreads) {
+        const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
+        const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
+        const float4 v = __ldg(&g4[gi]);
+        int pos0, p0, pos1, p1;
+        if constexpr (SLO == 2) { pos0 = 2 * row; pos1 = pos0 + 1; p0 = p1 = c; }
+        else { pos0 = pos1 = row; p0 = 2 * c; p1 = p0 + 1; }
+        float2 e0 = make_float2(v.x, v.y), e1 = make_float2(v.z, v.w);
+        if constexpr (DERIV) {
+            const float w0 = __ldg(&wpos[pos0]), w1 = __ldg(&wpos[pos1]);
+            e0 = cscale(mul_mi<false>(e0), w0);
+            e1 = cscale(mul_mi<false>(e1), w1);
+        }
+        s[V::at(pos0, p0)] = e0;
+        s[V::at(pos1, p1)] = e1;
+    }
+}
+
+template <int NT, int P, int SLO>
+__device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__ g, int q0, int NP, int tid) {
+    using V = PencilView<NT, P>;
+    constexpr int F4_PER_ROW = P * SLO / 2;
+    constexpr int ROWS = NT / SLO;
+    float4* g4 = reinterpret_cast<float4*>(g);
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += kThreads) {
+        const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
+        const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
+        int pos0, p0, pos1, p1;
+        if constexpr (SLO == 2) { pos0 = 2 * row; pos1 = pos0 + 1; p0 = p1 = c; }
+        else { pos0 = pos1 = row; p0 = 2 * c; p1 = p0 + 1; }
+        const float2 e0 = s[V::at(pos0, p0)], e1 = s[V::at(pos1, p1)];
+        g4[gi] = make_float4(e0.x, e0.y, e1.x, e1.y);
+    }
+}
+
+template <int NT, int P, int SLO, int MODE>
+__global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
+    using Cfg = PencilCfg<NT, P, SLO>;
+    using V = typename Cfg::View;
+    constexpr int TPP = Cfg::TPP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s = reinterpret_cast<float2*>(smem_raw);
+    void* scan_mem = smem_raw + Cfg::SMEM_FIELD;
+    double* tsum = reinterpret_cast<double*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN);
+    const int tid = threadIdx.x;
+    const int NP = args.NP;
+    const float2* tw = args.tw;
+
+    if constexpr (MODE == PM_TEMP) {
+        for (int t = tid; t < NT; t += kThreads) tsum[t] = 0.0;
+        __syncthreads();
+    }
+
+    for (int tile = blockIdx.x; tile < args.ntiles; tile += gridDim.x) {
+        const int q0 = tile * P;
+        if constexpr (MODE == PM_IONIZ) {
+            for (int f = tid; f < NT * P; f += kThreads) {
+                const int t = f / P, p = f - (f / P) * P;
+                const size_t gi = (size_t)t * NP + q0 + p;
+                const double2 v = __ldg(&reinterpret_cast<const double2*>(args.in)[gi]);
+                s[V::at(t, p)] = make_float2((float)(v.x * args.in_scale), (float)(v.y * args.in_scale));
+            }
+            __syncthreads();
+            nonlinear_tile<NT, P, true>(s, nullptr, args.nl, scan_mem, tid, args.tau_out, args.fe_out, q0, NP);
+            __syncthreads();
+        } else if constexpr (MODE == PM_ENTRY_C128 || MODE == PM_ENTRY_C64) {
+            // real-space input, reference layout A[t*NP + q]
+            for (int f = tid; f < NT * P; f += kThreads) {
+                const int t = f / P, p = f - (f / P) * P;
+                const size_t gi = (size_t)t * NP + q0 + p;
+                float2 e;
+                if constexpr (MODE == PM_ENTRY_C128) {
+                    const double2 v = __ldg(&reinterpret_cast<const double2*>(args.in)[gi]);
+                    e = make_float2((float)(v.x * args.in_scale), (float)(v.y * args.in_scale));
+                } else {
+                    e = cscale(__ldg(&reinterpret_cast<const float2*>(args.in)[gi]), (float)args.in_scale);
+                }
+                s[V::at(t, p)] = e;
+            }
+            __syncthreads();
+            dif_all<NT, NT, V>(s, tw, tid, kThreads);
+            store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
+            __syncthreads();
+        } else if constexpr (MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP) {
+            load_tile<NT, P, SLO, false>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
+            __syncthreads();
+            dit_all<NT, NT, V>(s, tw, tid, kThreads);
+            if constexpr (MODE == PM_TEMP) {
+                const double inv = args.out_scale * args.out_scale;
+                for (int t = tid; t < NT; t += kThreads) {
+                    float acc = 0.0f;
+#pragma unroll 8
+                    for (int p = 0; p < P; p++) {
+                        const float2 e = s[V::at(t, p)];
+                        acc = fmaf(e.x, e.x, fmaf(e.y, e.y, acc));
+                    }
+                    tsum[t] += (double)acc * inv;
+                }
+            } else {
+                for (int f = tid; f < NT * P; f += kThreads) {
+                    const int t = f / P, p = f - (f / P) * P;
+                    const size_t gi = (size_t)t * NP + q0 + p;
+                    const float2 e = s[V::at(t, p)];
+                    if constexpr (MODE == PM_EXIT_C128) {
+                        const double sc = args.out_scale;
+                        reinterpret_cast<double2*>(args.out)[gi] = make_double2((double)e.x * sc, (double)e.y * sc);
+                    } else {
+                        reinterpret_cast<float2*>(args.out)[gi] = cscale(e, (float)args.out_scale);
+                    }
+                }
+                // per-pencil energy sum_t |A|^2 (physical units)
+                if (args.pencil_energy) {
+                    const int p = tid % P, part = tid / P;           // kThreads/P partial sums per pencil
+                    constexpr int PARTS = kThreads / P;
+                    float acc = 0.0f;
+                    for (int t = part; t < NT; t += PARTS) {
+                        const float2 e = s[V::at(t, p)];
+                        acc = fmaf(e.x, e.x, fmaf(e.y, e.y, acc));
+                    }
+                    double* red = reinterpret_cast<double*>(scan_mem);
+                    __syncthreads();
+                    red[part * P + p] = (double)acc;
+                    __syncthreads();
+                    if (tid < P) {
+                        double tot = 0.0;
+                        for (int k = 0; k < PARTS; k++) tot += red[k * P + tid];
+                        args.pencil_energy[q0 + tid] = tot * args.out_scale * args.out_scale;
+                    }
+                }
+            }
+            __syncthreads();
+        } else {  // PM_STEP
+            const NLConst& c = args.nl;
+            float2* scr = args.scratch + (size_t)blockIdx.x * NT * P;
+            const float2* gin = reinterpret_cast<const float2*>(args.in);
+            // dA = IFFT_t(-i omega S): the time derivative term of the self-steepening
+            if (c.sst_c != 0.0f) {
+                load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
+                __syncthreads();
+                dit_all<NT, NT, V>(s, tw, tid, kThreads);
+                for (int f = tid; f < NT * P; f += kThreads) {
+                    const int t = f / P, p = f - (f / P) * P;
+                    scr[f] = s[V::at(t, p)];
+                }
+                __syncthreads();
+            }
+            // A = IFFT_t(S)
+            load_tile<NT, P, SLO, false>(s, gin, args.wpos, q0, NP, tid);
+            __syncthreads();
+            dit_all<NT, NT, V>(s, tw, tid, kThreads);
+
+            nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP);
+            __syncthreads();
+            dif_all<NT, NT, V>(s, tw, tid, kThreads);
+            store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
+            __syncthreads();
+        }
+    }
+    if constexpr (MODE == PM_TEMP) {
+        __syncthreads();
+        for (int t = tid; t < NT; t += kThreads) atomicAdd(&args.temp[t], tsum[t]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Plane pass
+// ---------------------------------------------------------------------------------------
+struct PlaneTables {
+    const float2* Rx;   // Nx, x position order
+    const float2* Ry;   // Ny, y position order
+    const float2* D;    // Nt, slot position order, includes 1/(Nx Ny Nt)
+};
+
+struct PlaneArgs {
+    const float2* in;
+    float2* out;
+    const float2* twx;
+    const float2* twy;
+    PlaneTables t1;      // first (or only) linear operator
+    PlaneTables t2;      // second half after the mirror lens (lens != 0)
+    const float2* lensx; // exp(-i k0 x^2 / roc), real x order
+    const float2* lensy;
+    int lens;            // 1: L(t1) -> lens -> L(t2)
+    int NP;
+    int nunits;          // number of cluster work units
+};
+
+template <int NX, int NY, int CL, int PB, int SLO>
+struct PlaneCfg {
+    static constexpr int RY = NY / CL;   // rows per CTA (row view)
+    static constexpr int CX = NX / CL;   // columns per CTA (column view)
+    static constexpr int RS = CX + 1;    // padded row stride
+    static constexpr int RSZ = PB * RY * RS;  // region (one partner block), complex64
+    static constexpr int SIZE = CL * RSZ;
+    static constexpr int SMEM = SIZE * 8 + (NX + NY) * 8;
+    static_assert(SLO == 1 || PB == SLO, "interleaved slots are processed together");
+    static_assert((RSZ % 2) == 0, "regions are moved as float4");
+};
+
+template <int NX, int NY, int CL, int PB, int SLO>
+struct RowView {
+    using C = PlaneCfg<NX, NY, CL, PB, SLO>;
+    static constexpr int NLINES = PB * C::RY;
+    static __device__ __forceinline__ int at(int x, int l) {
+        return (x / C::CX) * C::RSZ + l * C::RS + (x % C::CX);
+    }
+};
+template <int NX, int NY, int CL, int PB, int SLO>
+struct ColView {
+    using C = PlaneCfg<NX, NY, CL, PB, SLO>;
+    static constexpr int NLINES = PB * C::CX;
+    static __device__ __forceinline__ int at(int y, int l) {
+        const int pl = l / C::CX, xl = l - pl * C::CX;
+        return (y / C::RY) * C::RSZ + (pl * C::RY + (y % C::RY)) * C::RS + xl;
+    }
+};
+
+// Swap region g of this CTA with region `rank` of CTA g, for every g != rank.
+template <int CL, int RSZ>
+__device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& cluster, int rank, int tid) {
+    if constexpr (CL > 1) {
+        constexpr int F4 = RSZ / 2;               // float4 per region
+        constexpr int KR = (CL >= 4) ? 2 : 1;     // partners per round
+        constexpr int PER = (KR * F4 + kThreads - 1) / kThreads;
+        cluster.sync();
+        for (int k0 = 1; k0 < CL; k0 += KR) {
+            float4 buf[PER];
+#pragma unroll
+            for (int i = 0; i < PER; i++) {
+                const int f = tid + i * kThreads;
+                if (f < KR * F4) {
+                    const int kk = k0 + f / F4;
+                    if (kk < CL) {
+                        const int g = rank ^ kk;
+                        const float4* rem = reinterpret_cast<const float4*>(cluster.map_shared_rank(s, g));
+                        buf[i] = rem[rank * F4 + (f % F4)];
+                    }
+                }
+            }
+            cluster.sync();
+#pragma unroll
+            for (int i = 0; i < PER; i++) {
+                const int f = tid + i * kThreads;
+                if (f < KR * F4) {
+                    const int kk = k0 + f / F4;
+                    if (kk < CL) {
+                        const int g = rank ^ kk;
+                        reinterpret_cast<float4*>(s)[g * F4 + (f % F4)] = buf[i];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int NX, int NY, int CL, int PB, int SLO>
+__device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, const PlaneTables& T, int rank, int unit,
+                                             float2* tabx, cg::cluster_group& cluster, int tid) {
+    using C = PlaneCfg<NX, NY, CL, PB, SLO>;
+    using RV = RowView<NX, NY, CL, PB, SLO>;
+    using CV = ColView<NX, NY, CL, PB, SLO>;
+    dif_all<NX, NX, RV>(s, a.twx, tid, kThreads);
+    cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
+    dif_all<NY, NY, CV>(s, a.twy, tid, kThreads);
+    // multiply by Rx(px) Ry(py) D(slot)
+    for (int e = tid; e < PB * NY * C::CX; e += kThreads) {
+        const int xl = e % C::CX;
+        const int r = e / C::CX;
+        const int y = r % NY, pl = r / NY;
+        const int px = rank * C::CX + xl;
+        const int slot = (SLO == 1) ? unit * PB + pl : unit * SLO + pl;
+        const float2 f = cmul(cmul(__ldg(&T.Rx[px]), __ldg(&T.Ry[y])), __ldg(&T.D[slot]));
+        const int idx = CV::at(y, pl * C::CX + xl);
+        s[idx] = cmul(s[idx], f);
+    }
+    __syncthreads();
+    dit_all<NY, NY, CV>(s, a.twy, tid, kThreads);
+    cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
+    dit_all<NX, NX, RV>(s, a.twx, tid, kThreads);
+    (void)tabx;
+}
+
+template <int NX, int NY, int CL, int PB, int SLO>
+__global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
+    using C = PlaneCfg<NX, NY, CL, PB, SLO>;
+    using RV = RowView<NX, NY, CL, PB, SLO>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s = reinterpret_cast<float2*>(smem_raw);
+    float2* tabx = reinterpret_cast<float2*>(smem_raw + C::SIZE * 8);
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x;
+    const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;
+    const int NP = a.NP;
+
+    for (int unit = cid; unit < a.nunits; unit += ncl) {
+        // load this CTA's rows: y in [rank*RY, rank*RY + RY) of PB planes
+        constexpr int F4_ROW = NX * SLO / 2;
+        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += kThreads) {
+            const int c = f % F4_ROW;
+            const int r = f / F4_ROW;
+            const int yl = r % C::RY, plb = r / C::RY;  // plb: plane block (SLO == 1: plane)
+            const int y = rank * C::RY + yl;
+            size_t gi;
+            if constexpr (SLO == 1) gi = ((size_t)(unit * PB + plb) * NP + (size_t)y * NX) / 2 + c;
+            else gi = ((size_t)unit * NP * SLO + (size_t)y * NX * SLO) / 2 + c;
+            const float4 v = __ldg(reinterpret_cast<const float4*>(a.in) + gi);
+            if constexpr (SLO == 1) {
+                const int x = 2 * c;
+                s[RV::at(x, plb * C::RY + yl)] = make_float2(v.x, v.y);
+                s[RV::at(x + 1, plb * C::RY + yl)] = make_float2(v.z, v.w);
+            } else {
+                const int x = c;  // one float4 = both slots of one x
+                s[RV::at(x, 0 * C::RY + yl)] = make_float2(v.x, v.y);
+                s[RV::at(x, 1 * C::RY + yl)] = make_float2(v.z, v.w);
+            }
+        }
+        __syncthreads();
+        plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t1, rank, unit, tabx, cluster, tid);
+        if (a.lens) {
+            // mirror lens in real (x, y): exp(-i k0 (x^2 + y^2)/roc) = lensx[x] * lensy[y]
+            for (int e = tid; e < PB * C::RY * NX; e += kThreads) {
+                const int x = e % NX;
+                const int l = e / NX;
+                const int yl = l % C::RY;
+                const int y = rank * C::RY + yl;
+                const int idx = RV::at(x, l);
+                s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y])));
+            }
+            __syncthreads();
+            plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t2, rank, unit, tabx, cluster, tid);
+        }
+        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += kThreads) {
+            const int c = f % F4_ROW;
+            const int r = f / F4_ROW;
+            const int yl = r % C::RY, plb = r / C::RY;
+            const int y = rank * C::RY + yl;
+            size_t gi;
+            if constexpr (SLO == 1) gi = ((size_t)(unit * PB + plb) * NP + (size_t)y * NX) / 2 + c;
+            else gi = ((size_t)unit * NP * SLO + (size_t)y * NX * SLO) / 2 + c;
+            float2 e0, e1;
+            if constexpr (SLO == 1) {
+                const int x = 2 * c;
+                e0 = s[RV::at(x, plb * C::RY + yl)];
+                e1 = s[RV::at(x + 1, plb * C::RY + yl)];
+            } else {
+                e0 = s[RV::at(c, 0 * C::RY + yl)];
+                e1 = s[RV::at(c, 1 * C::RY + yl)];
+            }
+            reinterpret_cast<float4*>(a.out)[gi] = make_float4(e0.x, e0.y, e1.x, e1.y);
+        }
+        __syncthreads();
+    }
+    cluster.sync();
+}
+
+}  // namespace mpc

@@ -1,0 +1,67 @@
+// ref_wrap.cpp -- extern "C" entry points onto the reference's own functions, compiled
+// from the reference sources by oracle/build_ref.sh into oracle/_ref/libmpcref.so.
+//
+// TEST INFRASTRUCTURE ONLY: it exists to pin the oracle's restatement against the
+// reference's code (tests/golden/make_golden.py).  Only functions that are well defined on
+// their own are exposed: plasma.c's ionizpot, Natoms, ADK and ioniz, and propagation.c's
+// host-side calcexpR, fftshift (axis 0), calc1oes and setStep.
+#include <cstdlib>
+#include <cstring>
+
+#include "plasma.h"
+#include "propagation.h"
+
+extern "C" {
+
+void ref_ionizpot(const char* gas, double* I1, double* I2) { ionizpot(gas, I1, I2); }
+void ref_Natoms(const char* gas, double* Natm, double* sig) { Natoms(gas, Natm, sig); }
+
+void ref_ADK(long n, double* r1, double* r2, double* C_nl, double* f_lm, double* nq, double* mq, double* Ei,
+             double* E) {
+    int dims[3] = {(int)n, 1, 1};
+    ADK(r1, r2, dims, C_nl, f_lm, nq, mq, Ei, E);
+}
+
+// ioniz reads Iion[2] from a two-element heap block (plasma.c:276).  That value only feeds
+// the second-stage rate W2, which the as-written descending scan multiplies by zero; to keep
+// the run deterministic the 32-byte heap chunk that ioniz's malloc(2*sizeof(double)) will
+// reuse (glibc's per-thread cache returns the most recently freed chunk of that size) is
+// primed so that index 2 holds `iion2` (the second ionization potential in Hartree).
+void ref_ioniz(double* A, int Nx, int Ny, int Nt, double w0, double deltat, const char* gas, double rho_c,
+               double* w, double rho_nt, double n0, double* tau_c, double* fe, double iion2) {
+    int dims[3] = {Nx, Ny, Nt};
+    char g[16];
+    strncpy(g, gas, sizeof g - 1);
+    g[sizeof g - 1] = 0;
+    double* prime = (double*)malloc(3 * sizeof(double));
+    prime[0] = prime[1] = 0.0;
+    prime[2] = iion2;
+    free(prime);
+    ioniz(reinterpret_cast<cufftDoubleComplex*>(A), dims, w0, deltat, g, rho_c, w, rho_nt, n0, tau_c, fe);
+}
+
+void ref_calcexpR(double* expR, int* signmem, double z, double Cav, double k0, double dzz, double* wr, int Nx,
+                  int Ny) {
+    int dims[3] = {Nx, Ny, 1};
+    calcexpR(reinterpret_cast<cufftDoubleComplex*>(expR), signmem, z, Cav, k0, dzz, wr, dims);
+}
+
+void ref_fftshift0(double* v, int Nt) {
+    int dims[3] = {1, 1, Nt};
+    cufftDoubleComplex* buf = (cufftDoubleComplex*)malloc(sizeof(cufftDoubleComplex) * Nt);
+    fftshift(reinterpret_cast<cufftDoubleComplex*>(v), dims, buf, 0);
+    free(buf);
+}
+
+void ref_calc1oes(double* BP, int n, double* r, double* vald, double* y) {
+    int dims[3] = {n, n, 1};
+    calc1oes(BP, dims, r, vald, y);
+}
+
+void ref_setStep(long n, double* dzz, double* C1, double* C2, double def_err, double dzmin, double* y1, double* y2,
+                 int* bad, double* err) {
+    int dims[3] = {(int)n, 1, 1};
+    setStep(dims, dzz, reinterpret_cast<cufftDoubleComplex*>(C1), reinterpret_cast<cufftDoubleComplex*>(C2), def_err,
+            dzmin, y1, y2, bad, err);
+}
+}

@@ -1,0 +1,157 @@
+"""Parity of the CUDA path (through the C ABI of libmpc_gpu.so) against the FP64 CPU oracle.
+
+Tolerances: the device field is complex64 with FP32 FFTs; one split step reproduces the
+FP64 oracle to a relative L2 error of ~1e-6, so single-step checks use 1e-5 and runs of
+hundreds of steps 1e-4 (the accuracy target for the full 256^2 x 2048 run).  FP64 device
+routines (ADK) are checked to 1e-12.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mpc_gb300 import inputs
+from mpc_gb300.params import BOUNCE_LENS, BOUNCE_SIGNFLIP
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def small_cell(**kw):
+    base = dict(Nx=32, Ny=32, Nt=256, window_xy=4e-3, window_t=2e-12, energy=0.5e-3, steps_per_pass=50)
+    base.update(kw)
+    p, A = inputs.make_cell(inputs.config1(**base))
+    o = oracle.Oracle(p)
+    o.calibrate(A)
+    return p, A, o
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 64), (32, 32, 256), (64, 64, 512)])
+def test_linearstep(gpu_lib, shape):
+    from mpc_gb300.capi import Propagator
+    Nx, Ny, Nt = shape
+    p, A, o = small_cell(Nx=Nx, Ny=Ny, Nt=Nt, window_t=2e-12 * Nt / 256)
+    rng = np.random.default_rng(1)
+    A = A + 0.1 * np.abs(A).max() * (rng.standard_normal(A.size) + 1j * rng.standard_normal(A.size))
+    dz = 0.01
+    eD = o.expD0(dz)
+    eR, _ = o.calcexpR(Nx, 1, 0.0, dz / 2)
+    ref = A.copy()
+    oracle.lib().or_linearstep(oracle._p(ref.view(np.float64)), Nx, Ny, Nt, oracle._p(eD.view(np.float64)),
+                               oracle._p(eR.view(np.float64)), oracle._p(eR.view(np.float64)))
+    with Propagator(p) as prop:
+        got = A.copy()
+        prop.linearstep(got, eD, eR)
+    assert rel(got, ref) < 1e-5
+
+
+def test_calcexpR(gpu_lib):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell()
+    with Propagator(p) as prop:
+        for z, sm in [(0.1, 1), (0.6, 1), (0.6, -1), (1.2, -1)]:
+            ref, sm_ref = o.calcexpR(p.Nx, sm, z, 1.25e-3)
+            got, sm_got = prop.calcexpR(sm, z, 1.25e-3)
+            assert sm_got == sm_ref
+            assert np.abs(got - ref).max() < 2e-7
+
+
+def test_ADK_fp64(gpu_lib):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell()
+    E = np.geomspace(1e-4, 0.5, 257)
+    with Propagator(p) as prop:
+        r1, r2 = prop.ADK(E)
+    I1, I2 = oracle.ionizpot("Argon")
+    Iion = np.array([I1, I2]) / 27.21
+    nq = np.array([1 / np.sqrt(2 * Iion[0]), 2 / np.sqrt(2 * Iion[1])])
+    from math import gamma
+    Cnl = np.array([np.sqrt(2 ** (2 * n) / (n * gamma(n + 1) * gamma(n))) for n in nq])
+    e1, e2 = oracle.ADK(E, Cnl, [1, 1], nq, [0, 0], Iion)
+    assert rel(r1, e1) < 1e-12 and rel(r2, e2) < 1e-12
+
+
+def test_ioniz(gpu_lib):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(energy=3e-3, fwhm=120e-15, pressure=3.0, beam_w=0.3e-3)
+    tau_ref, fe_ref = o.ioniz(A)
+    with Propagator(p) as prop:
+        tau, fe = prop.ioniz(A)
+    assert rel(tau, tau_ref) < 1e-5
+    assert fe_ref.max() > 0
+    assert rel(fe, fe_ref) < 1e-4
+
+
+@pytest.mark.parametrize("plasm,sst", [(1, 1), (0, 1), (1, 0), (0, 0)])
+def test_ssfmprop_one_step(gpu_lib, plasm, sst):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(energy=3e-3, fwhm=120e-15, pressure=3.0, beam_w=0.3e-3, plasm=plasm, sst_on=sst)
+    ref = A.copy()
+    r_or = o.ssfmprop(ref, p.dzz, 1, 0.0, p.puls_e, change=1)
+    with Propagator(p) as prop:
+        got = A.copy()
+        r_gpu = prop.ssfmprop(got, p.dzz, 1, 0.0, p.puls_e, change=1)
+    assert rel(got, ref) < 1e-5
+    assert rel(r_gpu["BP1"], r_or["BP1"]) < 1e-5 and rel(r_gpu["BP2"], r_or["BP2"]) < 1e-5
+    assert np.allclose(r_gpu["y1"], r_or["y1"], rtol=1e-6) and r_gpu["signmem"] == r_or["signmem"]
+
+
+@pytest.mark.parametrize("bounce", [BOUNCE_LENS, BOUNCE_SIGNFLIP])
+def test_run_fixed_two_passes(gpu_lib, bounce):
+    """100 fixed steps (2 passes of 50, mirror bounce between them) on 32x32x256."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(energy=2e-3, fwhm=150e-15, pressure=2.0, bounce=bounce, steps_per_pass=50)
+    o2 = oracle.Oracle(p)
+    ref = A.copy()
+    st = o2.new_state()
+    o2.run_fixed(ref, st, 100)
+    with Propagator(p) as prop:
+        prop.upload(A)
+        prop.run_fixed(100)
+        got = prop.download()
+        s = prop.state()
+    assert s.nstep == 100 and abs(s.z - st.z) < 1e-12
+    assert rel(got, ref) < 1e-4
+    # spectrum
+    assert rel(np.abs(np.fft.fft(got.reshape(p.Nt, -1), axis=0)), np.abs(np.fft.fft(ref.reshape(p.Nt, -1), axis=0))) < 1e-4
+
+
+def test_diag(gpu_lib):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell()
+    with Propagator(p) as prop:
+        prop.upload(A)
+        temp, spec, BP1, BP2 = prop.diag()
+        energy = prop.energy()
+    t_ref, s_ref, b1, b2 = o.diag(A)
+    assert rel(temp, t_ref) < 1e-6 and rel(spec, s_ref) < 1e-6
+    assert rel(BP1, b1) < 1e-6 and rel(BP2, b2) < 1e-6
+    assert abs(energy / o.energy(A) - 1) < 1e-6
+
+
+def test_setStep(gpu_lib):
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell()
+    rng = np.random.default_rng(3)
+    for scale in (1e-7, 1e-5, 3e-5, 1e-3):
+        C1 = A.copy()
+        C2 = A + scale * np.abs(A).max() * rng.standard_normal(A.size)
+        y = np.array([0.0, 1e-3, 0, 0])
+        ref = oracle.setStep(1e-3, C1, C2, p.def_err, p.dzmin, y, y)
+        with Propagator(p) as prop:
+            got = prop.setStep(1e-3, C1, C2, y, y)
+        assert got[1] == ref[1] and abs(got[0] - ref[0]) < 1e-15 and abs(got[2] / ref[2] - 1) < 1e-12
+
+
+def test_energy_conservation_no_plasma(gpu_lib):
+    """Kerr + SST + dispersion + diffraction, alpha = 0, no plasma: energy is invariant."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(plasm=0, energy=2e-3)
+    with Propagator(p) as prop:
+        prop.upload(A)
+        e0 = prop.energy()
+        prop.run_fixed(100)
+        e1 = prop.energy()
+    assert abs(e1 / e0 - 1) < 2e-5

@@ -1,0 +1,148 @@
+"""Host-side logic that needs no GPU: the param.bin record, the seeded input generator, the
+position->frequency tables of the in-place FFT sweeps, and the C ABI library's exports."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from mpc_gb300 import inputs
+from mpc_gb300.params import MPCParams, read_field, write_field
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_param_bin_roundtrip(tmp_path):
+    p, A = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32))
+    path = tmp_path / "param.bin"
+    p.write(str(path))
+    raw = path.read_bytes()
+    # exact size of the record MPC.c reads field by field
+    Nx, Ny, Nt = p.dims
+    assert len(raw) == 3 * 4 + 2 * 8 + Nt * 8 + 3 * 8 + Ny * 8 + 4 + Nt * 8 + 2 * 8 + 4 + 6 * 8 + Ny * 8 + 4 * 8 + 9
+    q = MPCParams.read(str(path), bounce_mode=p.bounce_mode, roc=p.roc)
+    for f in ("dims", "dist", "dzz", "alpha", "Cav", "k0", "sst_on", "gamma2", "w0", "plasm", "deltat", "rho_c",
+              "rho_nt", "n0", "puls_e", "Ab_M", "dr", "def_err", "dzmin", "Esig", "gas"):
+        assert getattr(q, f) == getattr(p, f), f
+    for f in ("betas", "wr", "w", "r"):
+        np.testing.assert_array_equal(getattr(q, f), getattr(p, f))
+    write_field(str(tmp_path / "datar.bin"), str(tmp_path / "datai.bin"), A)
+    B = read_field(str(tmp_path / "datar.bin"), str(tmp_path / "datai.bin"), p.dims)
+    np.testing.assert_array_equal(A, B)
+
+
+def test_param_bin_rejects_truncated():
+    p, _ = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32))
+    with pytest.raises(Exception):
+        MPCParams.from_bytes(p.to_bytes()[:-20])
+
+
+def test_splitmix64_known_values():
+    # splitmix64 reference outputs for seed 0 (Vigna's reference implementation)
+    v = inputs.splitmix64(0, 3)
+    assert [int(x) for x in v] == [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
+
+
+def test_generator_deterministic_and_calibrated():
+    p1, A1 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=5))
+    p2, A2 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=5))
+    np.testing.assert_array_equal(A1, A2)
+    _, A3 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=6))
+    assert not np.array_equal(A1, A3)
+    HBAR = 1.054560652926899e-34
+    E = np.sum(np.abs(A1) ** 2) * p1.dr ** 2 * p1.deltat * HBAR * p1.w0
+    assert E == pytest.approx(p1.Esig, rel=1e-12)
+    noise = inputs.gaussian_noise(1, 200000)
+    assert abs(np.mean(np.abs(noise) ** 2) - 1) < 0.02
+
+
+def test_sweep_distribution():
+    cells = inputs.sweep_cells()
+    assert len(cells) == 64
+    e = np.array([c.energy for c in cells])
+    pr = np.array([c.pressure for c in cells])
+    fw = np.array([c.fwhm for c in cells])
+    assert e.min() >= 0.1e-3 and e.max() <= 2e-3 and pr.min() >= 0.5 and pr.max() <= 3 and fw.min() >= 100e-15
+    assert sum(c.Nx == 128 for c in cells) == 32 and sum(c.Nt == 512 for c in cells) == 32
+
+
+def _freq_of_pos(N):
+    """Python statement of the in-place DIF sweep with radices 16...16, r_last, run on
+    delta functions: which frequency ends up at which position."""
+    radix, span = [], []
+    L = N
+    while L > 1:
+        R = 16 if L >= 16 else L
+        radix.append(R)
+        span.append(L // R)
+        L //= R
+    x = np.eye(N, dtype=np.complex128)
+    for s, R in enumerate(radix):
+        Ls = span[s] * R
+        out = x.copy()
+        for b in range(N // Ls):
+            for j in range(span[s]):
+                idx = b * Ls + j + span[s] * np.arange(R)
+                v = x[idx]
+                y = np.fft.fft(v, axis=0)
+                y *= np.exp(-2j * np.pi * j * np.arange(R) / Ls)[:, None]
+                out[idx] = y
+        x = out
+    # row = position, column = input index; X[pos] = sum_n x_n W^(n f) identifies f
+    f = []
+    for pos in range(N):
+        ph = np.angle(x[pos, 1]) if N > 1 else 0.0
+        f.append(int(round(-ph * N / (2 * np.pi))) % N)
+        np.testing.assert_allclose(x[pos], np.exp(-2j * np.pi * np.arange(N) * f[-1] / N), atol=1e-9)
+    return f
+
+
+@pytest.mark.parametrize("N", [8, 64, 128, 512, 2048])
+def test_position_frequency_table(N):
+    """The closed form the library uses (pos = sum span_s k_s, freq = sum k_s prod r_<s)
+    matches a direct simulation of the DIF sweep."""
+    radix, span = [], []
+    L = N
+    while L > 1:
+        R = 16 if L >= 16 else L
+        radix.append(R)
+        span.append(L // R)
+        L //= R
+    closed = []
+    for pos in range(N):
+        rem, freq, mult = pos, 0, 1
+        for s in range(len(radix)):
+            k = rem // span[s]
+            rem -= k * span[s]
+            freq += k * mult
+            mult *= radix[s]
+        closed.append(freq)
+    if N <= 512:
+        assert closed == _freq_of_pos(N)
+    assert sorted(closed) == list(range(N))
+
+
+def _header_symbols():
+    with open(os.path.join(ROOT, "include", "mpc_gpu.h")) as f:
+        txt = f.read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mpc_[a-z0-9_A-Z]+)\s*\(", txt)))
+
+
+def test_capi_library_exports_every_header_symbol():
+    """libmpc_gpu.so loads without a GPU and exports every entry point of include/mpc_gpu.h;
+    no compute call is made here."""
+    from mpc_gb300 import build, capi
+    lib_path = build.build()
+    lib = C.CDLL(lib_path)
+    syms = _header_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) <= set(capi.SIGNATURES), set(syms) - set(capi.SIGNATURES)
+    lib.mpc_version.restype = C.c_char_p
+    assert b"sm_103a" in lib.mpc_version()
+    lib.mpc_shape_supported.argtypes = [C.c_int] * 3
+    assert lib.mpc_shape_supported(256, 256, 2048) == 1
+    assert lib.mpc_shape_supported(100, 100, 100) == 0
