@@ -14,7 +14,7 @@ import numpy as np
 from .params import MPCParams
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libmpc_gpu.so")
+LIB_PATH = os.environ.get("MPC_GPU_LIB", os.path.join(_HERE, "libmpc_gpu.so"))
 
 MPC_OK = 0
 ERRORS = {1: "MPC_ERR_ARG", 2: "MPC_ERR_SHAPE", 3: "MPC_ERR_CUDA", 4: "MPC_ERR_NOMEM", 5: "MPC_ERR_NONFINITE",

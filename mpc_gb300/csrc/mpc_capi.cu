@@ -66,31 +66,49 @@ struct TabIn {
     double zd, zp, k0, alpha, scale;
 };
 
-// Rx[px] = exp(-i zd kap^2/(2 k0)), kap = wr[m] - wr[N/2], m = centred index of freq(px);
-// D[pos] = scale * exp(zp (i beta[m] - alpha/2)).  Phase arguments and their range
-// reduction in FP64 (propagation.c:375-391, kernels.cu:47-54, corrected).
-__global__ void k_tables(TabIn in, float2* Rx, float2* Ry, float2* D) {
+// FP64 factors of one linear step (propagation.c:375-391 and kernels.cu:47-54, corrected):
+//   Rx[px] = exp(-i zd kap^2 / (2 k0)), kap = wr[m] - wr[N/2], m = centred index of freq(px);
+//   D[pos] = scale * exp(zp (i beta[m] - alpha/2)).
+// Phase arguments and their range reduction in FP64.
+__global__ void k_phase64(TabIn in, double2* Rx, double2* Ry, double2* D) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < in.Nx) {
         const int m = (in.fx[i] + in.Nx / 2) % in.Nx;
         const double kap = in.wr[m] - in.wr[in.Nx / 2];
         double s, c;
         sincos(-in.zd * kap * kap / (2.0 * in.k0), &s, &c);
-        Rx[i] = make_float2((float)c, (float)s);
+        Rx[i] = make_double2(c, s);
     }
     if (i < in.Ny) {
         const int m = (in.fy[i] + in.Ny / 2) % in.Ny;
         const double kap = in.wr[m] - in.wr[in.Ny / 2];
         double s, c;
         sincos(-in.zd * kap * kap / (2.0 * in.k0), &s, &c);
-        Ry[i] = make_float2((float)c, (float)s);
+        Ry[i] = make_double2(c, s);
     }
     if (i < in.Nt) {
         const int m = (in.ft[i] + in.Nt / 2) % in.Nt;
         const double amp = exp(-in.zp * in.alpha / 2.0) * in.scale;
         double s, c;
         sincos(in.zp * in.betas[m], &s, &c);
-        D[i] = make_float2((float)(amp * c), (float)(amp * s));
+        D[i] = make_double2(amp * c, amp * s);
+    }
+}
+
+__device__ __forceinline__ float4 split_df(double2 z) {
+    const float hx = (float)z.x, hy = (float)z.y;
+    return make_float4(hx, hy, (float)(z.x - (double)hx), (float)(z.y - (double)hy));
+}
+
+// Double-float tables of the plane sweep: Rx_df[px] and RyD_df[y * Nt + pos] = Ry[y] D[pos]
+// (the product formed in FP64).
+__global__ void k_split(const double2* Rx, const double2* Ry, const double2* D, int Nx, int Ny, int Nt,
+                        float4* Rx_df, float4* RyD_df) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < Nx) Rx_df[i] = split_df(Rx[i]);
+    if (i < (long)Ny * Nt) {
+        const double2 a = Ry[i / Nt], b = D[i % Nt];
+        RyD_df[i] = split_df(make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x));
     }
 }
 
@@ -191,9 +209,9 @@ __global__ void k_adk(long n, const double* __restrict__ E, double* r1, double* 
 // context
 // ---------------------------------------------------------------------------------------
 struct TableSet {
-    float2* Rx = nullptr;
-    float2* Ry = nullptr;
-    float2* D = nullptr;
+    float4* Rx = nullptr;       // double-float Rx, Nx
+    float4* RyD = nullptr;      // double-float Ry x D, Ny * Nt
+    double2* f64 = nullptr;     // FP64 Rx (Nx), Ry (Ny), D (Nt); base of the allocation
 };
 
 struct mpc_ctx {
@@ -214,7 +232,7 @@ struct mpc_ctx {
     float2* scratch = nullptr;
     double2* io = nullptr;      // complex128 staging, N
     double2* io2 = nullptr;     // second complex128 staging (setStep)
-    float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;
+    float4 *twx = nullptr, *twy = nullptr, *twt = nullptr;
     float* wpos = nullptr;
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
     std::vector<int> hfx, hfy, hft;
@@ -286,14 +304,17 @@ static std::vector<int> freq_of_pos(int N) {
     return f;
 }
 
-static int upload_twiddles(int N, float2** d) {
-    std::vector<float2> h(N);
+// W_N^k rounded to FP32 from FP64, plus -(|W|^2 - 1) of the rounded value (see mpc_fft.cuh)
+static int upload_twiddles(int N, float4** d) {
+    std::vector<float4> h(N);
     for (int k = 0; k < N; k++) {
         const double a = -2.0 * M_PI * (double)k / (double)N;
-        h[k] = make_float2((float)cos(a), (float)sin(a));
+        const float c = (float)cos(a), s = (float)sin(a);
+        const double eps = (double)c * c + (double)s * s - 1.0;
+        h[k] = make_float4(c, s, (float)-eps, 0.0f);
     }
-    CK(cudaMalloc(d, sizeof(float2) * N), "cudaMalloc twiddles");
-    CK(cudaMemcpy(*d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "copy twiddles");
+    CK(cudaMalloc(d, sizeof(float4) * N), "cudaMalloc twiddles");
+    CK(cudaMemcpy(*d, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice), "copy twiddles");
     return MPC_OK;
 }
 
@@ -334,7 +355,9 @@ static void build_nl(mpc_ctx* c) {
     c->sst_c_full = (float)(p.gamma2 / (p.w0 * fs2));
     n.sst_c = p.sst_on == 1 ? c->sst_c_full : 0.0f;
     n.I_scale = (float)I_UNIT;
-    n.E_c = (float)(sqrt(2.0 * ZW0 / NC) * FCTR / EF);
+    const double E_c = sqrt(2.0 * ZW0 / NC) * FCTR / EF;  // plasma.c:145-149
+    n.E_c = (float)E_c;
+    n.inv_E_c = (float)(1.0 / E_c);
     double I1 = 0, I2 = 0, Natm = 0, sig = 0;
     c->ion_gas_ok = gas_tables(p.gas, &I1, &I2, &Natm, &sig);
     c->I1 = I1;
@@ -347,22 +370,44 @@ static void build_nl(mpc_ctx* c) {
         K1[s] = Cnl * Cnl * sqrt(6.0 / M_PI) * 1.0 * Iion[s];
         K3[s] = 2.0 * pow(2.0 * Iion[s], 1.5);
         K5[s] = 2.0 * nq[s] - 0.0 - 1.5;
-        n.lnK1[s] = (float)log(K1[s]);
-        n.K3[s] = (float)K3[s];
-        n.lnK3[s] = (float)log(K3[s]);
+        n.l2K1[s] = (float)log2(K1[s]);
+        n.l2K3[s] = (float)log2(K3[s]);
         n.K5[s] = (float)K5[s];
+        n.K3l2e[s] = (float)(K3[s] / (3.0 * M_LN2));
     }
     c->adk = ADKConst{K1[0], K1[1], K3[0], K3[1], K5[0], K5[1]};
-    n.Kon = (float)(p.deltat / T0);
-    n.ve_c = (float)(EL0 * EF / (sqrt(2.0) * ME * p.w0));
-    n.K3c = (float)(sig * p.rho_nt);
+    const double Kon = p.deltat / T0;
+    n.Kon = (float)Kon;
+    // v_e = sqrt(2 e^2 E0^2 / (4 me^2 w0^2)) with E0 = F EF (plasma.c:203, A18: w0 only)
+    n.Kuv = (float)(sig * p.rho_nt * EL0 * EF / (sqrt(2.0) * ME * p.w0));
     const double k0ion = p.w0 / C0;  // plasma.c:141
     n.K4w0 = (float)(k0ion / (p.n0 * p.rho_c) * p.w0 * p.w0);
     n.w0sq = (float)(p.w0 * p.w0);
     n.inv_w0 = (float)(1.0 / p.w0);
-    n.inv_I1 = I1 > 0 ? (float)(1.0 / I1) : 0.0f;
+    n.invI1_Kon = I1 > 0 ? (float)(Kon / I1) : 0.0f;
     n.rho_half = (float)(p.rho_nt / 2.0);
     n.plasma = (p.plasm == 1) ? 1 : 0;
+}
+
+// one allocation: FP64 factors (Nx + Ny + Nt double2), double-float Rx (Nx) and RyD (Ny*Nt)
+static int alloc_tables(mpc_ctx* c, TableSet* t) {
+    const size_t n64 = (size_t)(c->Nx + c->Ny + c->Nt);
+    const size_t bytes = n64 * sizeof(double2) + ((size_t)c->Nx + (size_t)c->Ny * c->Nt) * sizeof(float4);
+    char* buf = nullptr;
+    CK(cudaMalloc(&buf, bytes), "cudaMalloc tables");
+    t->f64 = reinterpret_cast<double2*>(buf);
+    t->Rx = reinterpret_cast<float4*>(buf + n64 * sizeof(double2));
+    t->RyD = t->Rx + c->Nx;
+    return MPC_OK;
+}
+
+static int split_tables(mpc_ctx* c, const TableSet& t) {
+    const long n = (long)c->Ny * c->Nt;
+    k_split<<<(int)((n + 255) / 256), 256, 0, c->st>>>(t.f64, t.f64 + c->Nx, t.f64 + c->Nx + c->Ny, c->Nx, c->Ny,
+                                                       c->Nt, t.Rx, t.RyD);
+    CK(cudaGetLastError(), "k_split");
+    c->launches++;
+    return MPC_OK;
 }
 
 static int get_tables(mpc_ctx* c, double zd, double zp, double scale, TableSet* out) {
@@ -374,21 +419,17 @@ static int get_tables(mpc_ctx* c, double zd, double zp, double scale, TableSet* 
     }
     if (c->tables.size() > 64) {  // adaptive runs: recycle the cache
         cudaStreamSynchronize(c->st);
-        for (auto& kv : c->tables) {
-            cudaFree(kv.second.Rx);
-        }
+        for (auto& kv : c->tables) cudaFree(kv.second.f64);
         c->tables.clear();
     }
     TableSet t;
-    float2* buf = nullptr;
-    CK(cudaMalloc(&buf, sizeof(float2) * (c->Nx + c->Ny + c->Nt)), "cudaMalloc tables");
-    t.Rx = buf;
-    t.Ry = buf + c->Nx;
-    t.D = buf + c->Nx + c->Ny;
+    int rc = alloc_tables(c, &t);
+    if (rc) return rc;
     TabIn in{c->dwr, c->dbetas, c->dfx, c->dfy, c->dft, c->Nx, c->Ny, c->Nt, zd, zp, c->p.k0, c->p.alpha, scale};
     const int n = c->Nt > c->Nx ? c->Nt : c->Nx;
-    k_tables<<<(n + 255) / 256, 256, 0, c->st>>>(in, (float2*)t.Rx, (float2*)t.Ry, (float2*)t.D);
-    CK(cudaGetLastError(), "k_tables");
+    k_phase64<<<(n + 255) / 256, 256, 0, c->st>>>(in, t.f64, t.f64 + c->Nx, t.f64 + c->Nx + c->Ny);
+    CK(cudaGetLastError(), "k_phase64");
+    if ((rc = split_tables(c, t))) return rc;
     c->launches++;
     c->tables[key] = t;
     *out = t;
@@ -415,9 +456,9 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     a.out = out;
     a.twx = c->twx;
     a.twy = c->twy;
-    a.t1 = PlaneTables{t1.Rx, t1.Ry, t1.D};
+    a.t1 = PlaneTables{t1.Rx, t1.RyD};
     if (t2) {
-        a.t2 = PlaneTables{t2->Rx, t2->Ry, t2->D};
+        a.t2 = PlaneTables{t2->Rx, t2->RyD};
         a.lens = 1;
     } else {
         a.t2 = a.t1;
@@ -425,6 +466,7 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     }
     a.lensx = c->lensx;
     a.lensy = c->lensy;
+    a.Nt = c->Nt;
     a.NP = (int)c->NP;
     a.nunits = c->ops->SLO == 2 ? c->Nt / 2 : c->Nt / c->ops->PB;
     cudaEvent_t ev;
@@ -456,8 +498,8 @@ int mpc_destroy(mpc_ctx* c) {
     if (!c) return MPC_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     prof_clear(c);
-    for (auto& kv : c->tables) cudaFree(kv.second.Rx);
-    if (c->ident.Rx) cudaFree(c->ident.Rx);
+    for (auto& kv : c->tables) cudaFree(kv.second.f64);
+    if (c->ident.f64) cudaFree(c->ident.f64);
     void* ptrs[] = {c->S, c->scratch, c->io, c->io2, c->twx, c->twy, c->twt, c->wpos, c->dfx, c->dfy,
                     c->dft, c->dwr, c->dbetas, c->dr, c->lensx, c->lensy, c->penergy, c->dred};
     for (void* q : ptrs)
@@ -564,14 +606,13 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
     // reductions: temp [0, Nt), spec [Nt, 2 Nt), beam profiles and sums use the front
     TRYC(cudaMalloc(&c->dred, sizeof(double) * (2 * Nt + Nx + Ny + 64)), "cudaMalloc reductions");
     {
-        float2* buf = nullptr;
-        TRYC(cudaMalloc(&buf, sizeof(float2) * (Nx + Ny + Nt)), "cudaMalloc identity tables");
-        c->ident = TableSet{buf, buf + Nx, buf + Nx + Ny};
+        TRY(alloc_tables(c, &c->ident));
         TabIn in{c->dwr, c->dbetas, c->dfx, c->dfy, c->dft, Nx, Ny, Nt, 0.0, 0.0, p->k0, p->alpha,
                  1.0 / (double)c->NP};
         const int n = Nt > Nx ? Nt : Nx;
-        k_tables<<<(n + 255) / 256, 256, 0, c->st>>>(in, buf, buf + Nx, buf + Nx + Ny);
-        TRYC(cudaGetLastError(), "k_tables identity");
+        k_phase64<<<(n + 255) / 256, 256, 0, c->st>>>(in, c->ident.f64, c->ident.f64 + Nx, c->ident.f64 + Nx + Ny);
+        TRYC(cudaGetLastError(), "k_phase64 identity");
+        TRY(split_tables(c, c->ident));
     }
     TRYC(cudaStreamSynchronize(c->st), "context setup");
     c->state.dzz = p->dzz;
@@ -828,29 +869,35 @@ int mpc_linearstep(mpc_ctx* c, double* A, const double* exp_D0, const double* ex
     if (!c || !A || !exp_D0 || !expR) return fail(MPC_ERR_ARG, "null argument");
     int rc = ensure_io(c, 0);
     if (rc) return rc;
-    // caller tables -> position order, conj(expR) along x and y, D scaled by 1/(Nx Ny)
+    // caller tables (FP64) -> position order, conj(expR) along x and y, D scaled by 1/(Nx Ny);
+    // reordering only on the host, the double-float split on the device
     const int Nx = c->Nx, Ny = c->Ny, Nt = c->Nt;
-    std::vector<float2> h(Nx + Ny + Nt);
+    std::vector<double2> h(Nx + Ny + Nt);
     for (int i = 0; i < Nx; i++) {
         const int f = c->hfx[i];
-        h[i] = make_float2((float)expR[2 * f], (float)-expR[2 * f + 1]);
+        h[i] = make_double2(expR[2 * f], -expR[2 * f + 1]);
     }
     for (int j = 0; j < Ny; j++) {
         const int f = c->hfy[j];
-        h[Nx + j] = make_float2((float)expR[2 * f], (float)-expR[2 * f + 1]);
+        h[Nx + j] = make_double2(expR[2 * f], -expR[2 * f + 1]);
     }
     const double sc = 1.0 / (double)c->NP;
     for (int k = 0; k < Nt; k++) {
         const int f = c->hft[k];
-        h[Nx + Ny + k] = make_float2((float)(exp_D0[2 * f] * sc), (float)(exp_D0[2 * f + 1] * sc));
+        h[Nx + Ny + k] = make_double2(exp_D0[2 * f] * sc, exp_D0[2 * f + 1] * sc);
     }
-    float2* buf = nullptr;
-    CK(cudaMalloc(&buf, sizeof(float2) * h.size()), "cudaMalloc caller tables");
-    cudaError_t e = cudaMemcpyAsync(buf, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice, c->st);
-    TableSet t{buf, buf + Nx, buf + Nx + Ny};
+    TableSet t;
+    if ((rc = alloc_tables(c, &t))) return rc;
+    cudaError_t e = cudaMemcpyAsync(t.f64, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice, c->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess && (rc = split_tables(c, t))) {
+        cudaStreamSynchronize(c->st);
+        cudaFree(t.f64);
+        return rc;
+    }
     if (e != cudaSuccess) {
-        cudaFree(buf);
+        cudaStreamSynchronize(c->st);
+        cudaFree(t.f64);
         return fail(MPC_ERR_CUDA, "H2D linearstep", e);
     }
     PencilArgs a{};
@@ -866,7 +913,7 @@ int mpc_linearstep(mpc_ctx* c, double* A, const double* exp_D0, const double* ex
         if (e != cudaSuccess) rc = fail(MPC_ERR_CUDA, "linearstep", e);
     }
     cudaStreamSynchronize(c->st);
-    cudaFree(buf);
+    cudaFree(t.f64);
     c->have_field = 1;
     return rc;
 }
@@ -879,8 +926,8 @@ int mpc_calcexpR(mpc_ctx* c, double* expR, int* signmem, double z, double dzz) {
     TableSet t;
     int rc = get_tables(c, signum * dzz, 0.0, 1.0, &t);
     if (rc) return rc;
-    std::vector<float2> h(c->Nx);
-    CK(cudaMemcpyAsync(h.data(), t.Rx, sizeof(float2) * c->Nx, cudaMemcpyDeviceToHost, c->st), "D2H table");
+    std::vector<double2> h(c->Nx);
+    CK(cudaMemcpyAsync(h.data(), t.f64, sizeof(double2) * c->Nx, cudaMemcpyDeviceToHost, c->st), "D2H table");
     CK(cudaStreamSynchronize(c->st), "calcexpR");
     // the device table is conj(expR) in position order; the reference returns expR in FFT order
     for (int px = 0; px < c->Nx; px++) {

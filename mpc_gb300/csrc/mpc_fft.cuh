@@ -31,19 +31,39 @@ template <bool INV>
 __device__ __forceinline__ float2 mul_mi(float2 a) {
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
+// The butterflies' constant factors (sqrt(1/2), cos(pi/8), sin(pi/8)) are applied as a high
+// FP32 part plus a low correction (exact value minus high part, from FP64).  Rounded to FP32
+// alone they are off unit modulus by 3e-8..6e-8, and since every forward/inverse round trip
+// applies the same constants, that error would accumulate linearly over the steps of a run
+// (about -2e-7 energy per split step); with the low parts it is ~1e-15.
+constexpr double kSqrtHalf = 0.70710678118654752440;
+constexpr double kCos8 = 0.92387953251128675613;   // cos(pi/8)
+constexpr double kSin8 = 0.38268343236508977173;   // sin(pi/8)
+constexpr float kH = (float)kSqrtHalf, kHl = (float)(kSqrtHalf - (double)(float)kSqrtHalf);
+constexpr float kC8 = (float)kCos8, kC8l = (float)(kCos8 - (double)(float)kCos8);
+constexpr float kS8 = (float)kSin8, kS8l = (float)(kSin8 - (double)(float)kSin8);
+
+// t * sqrt(1/2) with the low-part correction
+__device__ __forceinline__ float mul_h(float t) { return fmaf(t, kH, t * kHl); }
+
+// a * (z.hi + z.lo): double-float complex factor z = (x, y) + (z, w)
+__device__ __forceinline__ float2 cmul_df(float2 a, float4 z) {
+    const float cr = fmaf(a.x, z.z, -a.y * z.w);
+    const float ci = fmaf(a.x, z.w, a.y * z.z);
+    return make_float2(fmaf(a.x, z.x, fmaf(-a.y, z.y, cr)), fmaf(a.x, z.y, fmaf(a.y, z.x, ci)));
+}
+
 // multiply by exp(-+i*pi/4) = (1 -+ i)/sqrt(2)
 template <bool INV>
 __device__ __forceinline__ float2 mul_w8(float2 a) {
-    const float h = 0.70710678118654752f;
-    return INV ? make_float2((a.x - a.y) * h, (a.x + a.y) * h)
-               : make_float2((a.x + a.y) * h, (a.y - a.x) * h);
+    return INV ? make_float2(mul_h(a.x - a.y), mul_h(a.x + a.y))
+               : make_float2(mul_h(a.x + a.y), mul_h(a.y - a.x));
 }
 // multiply by exp(-+3i*pi/4) = (-1 -+ i)/sqrt(2)
 template <bool INV>
 __device__ __forceinline__ float2 mul_w83(float2 a) {
-    const float h = 0.70710678118654752f;
-    return INV ? make_float2((-a.x - a.y) * h, (a.x - a.y) * h)
-               : make_float2((a.y - a.x) * h, (-a.x - a.y) * h);
+    return INV ? make_float2(mul_h(-a.x - a.y), mul_h(a.x - a.y))
+               : make_float2(mul_h(a.y - a.x), mul_h(-a.x - a.y));
 }
 
 // ---- small DFTs in registers, natural order in and out, unnormalised ------------------
@@ -104,20 +124,19 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
 #pragma unroll
     for (int n2 = 0; n2 < 4; n2++) dft4<INV>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
     // now v[n2 + 4 k1] = Y[n2][k1]
-    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f;
     const float sg = INV ? 1.0f : -1.0f;
-    const float2 w1 = make_float2(c1, sg * s1);   // W16^1
-    const float2 w3 = make_float2(s1, sg * c1);   // W16^3
-    const float2 w9 = make_float2(-c1, -sg * s1); // W16^9
-    v[5] = cmul(v[5], w1);            // n2=1,k1=1
+    const float4 w1 = make_float4(kC8, sg * kS8, kC8l, sg * kS8l);      // W16^1
+    const float4 w3 = make_float4(kS8, sg * kC8, kS8l, sg * kC8l);      // W16^3
+    const float4 w9 = make_float4(-kC8, -sg * kS8, -kC8l, -sg * kS8l);  // W16^9
+    v[5] = cmul_df(v[5], w1);         // n2=1,k1=1
     v[9] = mul_w8<INV>(v[9]);         // n2=1,k1=2 : W16^2
-    v[13] = cmul(v[13], w3);          // n2=1,k1=3
+    v[13] = cmul_df(v[13], w3);       // n2=1,k1=3
     v[6] = mul_w8<INV>(v[6]);         // n2=2,k1=1 : W16^2
     v[10] = mul_mi<INV>(v[10]);       // n2=2,k1=2 : W16^4
     v[14] = mul_w83<INV>(v[14]);      // n2=2,k1=3 : W16^6
-    v[7] = cmul(v[7], w3);            // n2=3,k1=1
+    v[7] = cmul_df(v[7], w3);         // n2=3,k1=1
     v[11] = mul_w83<INV>(v[11]);      // n2=3,k1=2 : W16^6
-    v[15] = cmul(v[15], w9);          // n2=3,k1=3
+    v[15] = cmul_df(v[15], w9);       // n2=3,k1=3
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
     // now v[4 k1 + k2] = X[k1 + 4 k2]; transpose to natural order
@@ -142,11 +161,20 @@ struct Radix {
 // ---- batched in-place stages over a shared-memory view --------------------------------
 // View: NLINES independent lines of length N; element `pos` of line `l` lives at
 // V::at(pos, l).  Work items are (line, butterfly) pairs, lines fastest across threads.
-// tw: W_N^k = exp(-2 pi i k / N), k < N, complex64 rounded from FP64.
+// tw: twiddle table in shared memory, entry k = {c, s, -eps, 0} with (c, s) = W_N^k =
+// exp(-2 pi i k / N) rounded to FP32 from FP64 and eps = c^2 + s^2 - 1 (computed in FP64 from
+// the rounded values).  The forward (DIF) stage multiplies by (c, s); the inverse (DIT) stage
+// by conj(c, s) * (1 - eps), so every forward/inverse round trip has gain 1 - eps^2 per path
+// instead of 1 + eps: rounded twiddles alone lose ~6e-8 of the energy per split step.
 //
+// Every view used here is "stage separable": for a butterfly of span S starting at
+// base = b*L + j (j < S), V::at(base + S*q, l) == V::at(base, l) + V::at(S*q, 0) - V::at(0, 0),
+// so the R addresses of a butterfly are one computed base plus compile-time offsets
+// (tests/test_host.py checks the property for every view and stage of the library).
+
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
 template <int N, int L, class V>
-__device__ __forceinline__ void dif_stage(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dif_stage(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -155,23 +183,27 @@ __device__ __forceinline__ void dif_stage(float2* s, const float2* __restrict__ 
         const int line = idx % V::NLINES;
         const int g = idx / V::NLINES;
         const int b = g / S, j = g - (g / S) * S;
-        const int base = b * L + j;
+        float2* p0 = s + V::at(b * L + j, line);
         float2 v[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = s[V::at(base + S * q, line)];
+        for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         dft<R, false>(v);
         if (S > 1) {
+            const float4* t = tw + j * (N / L);
 #pragma unroll
-            for (int k = 1; k < R; k++) v[k] = cmul(v[k], __ldg(&tw[j * k * (N / L)]));
+            for (int k = 1; k < R; k++) {
+                const float4 w = t[j * (k - 1) * (N / L)];
+                v[k] = cmul(v[k], make_float2(w.x, w.y));
+            }
         }
 #pragma unroll
-        for (int q = 0; q < R; q++) s[V::at(base + S * q, line)] = v[q];
+        for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
     }
 }
 
 // DIT stage (exact transpose of the DIF stage with conjugate twiddles).
 template <int N, int L, class V>
-__device__ __forceinline__ void dit_stage(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dit_stage(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -180,23 +212,28 @@ __device__ __forceinline__ void dit_stage(float2* s, const float2* __restrict__ 
         const int line = idx % V::NLINES;
         const int g = idx / V::NLINES;
         const int b = g / S, j = g - (g / S) * S;
-        const int base = b * L + j;
+        float2* p0 = s + V::at(b * L + j, line);
         float2 v[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = s[V::at(base + S * q, line)];
+        for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         if (S > 1) {
+            const float4* t = tw + j * (N / L);
 #pragma unroll
-            for (int k = 1; k < R; k++) v[k] = cmulc(v[k], __ldg(&tw[j * k * (N / L)]));
+            for (int k = 1; k < R; k++) {
+                const float4 w = t[j * (k - 1) * (N / L)];
+                const float2 u = cmulc(v[k], make_float2(w.x, w.y));
+                v[k] = make_float2(fmaf(u.x, w.z, u.x), fmaf(u.y, w.z, u.y));
+            }
         }
         dft<R, true>(v);
 #pragma unroll
-        for (int q = 0; q < R; q++) s[V::at(base + S * q, line)] = v[q];
+        for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
     }
 }
 
 // Whole forward transform (natural -> position order).  Ends with a __syncthreads.
 template <int N, int L, class V>
-__device__ __forceinline__ void dif_all(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dif_all(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
     dif_stage<N, L, V>(s, tw, tid, nthr);
     __syncthreads();
     constexpr int R = Radix<L>::R;
@@ -205,7 +242,7 @@ __device__ __forceinline__ void dif_all(float2* s, const float2* __restrict__ tw
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
 template <int N, int L, class V>
-__device__ __forceinline__ void dit_all(float2* s, const float2* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dit_all(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     if constexpr (L / R > 1) dit_all<N, L / R, V>(s, tw, tid, nthr);
     dit_stage<N, L, V>(s, tw, tid, nthr);

@@ -26,6 +26,12 @@ namespace cg = cooperative_groups;
 namespace mpc {
 
 constexpr int kThreads = 512;          // both sweeps
+// L2 prefetch of the next pencil tile: measured slower on GB300 (it evicts the dA scratch
+// tiles from L2), so off by default
+#ifndef MPC_PREFETCH
+#define MPC_PREFETCH 0
+#endif
+constexpr bool kPrefetch = MPC_PREFETCH != 0;
 constexpr int kTilePoints = 16384;     // pencil tile: P * Nt complex points (128 KB)
 
 // FP32 constants of the nonlinear step, computed on the host in FP64.
@@ -35,14 +41,14 @@ struct NLConst {
     float sst_c;     // gamma2 / (w0 fs^2), 0 when self-steepening is off
     float I_scale;   // intensity [W/m^2] per unit |a|^2
     float E_c;       // field in atomic units = sqrt(I) * E_c
-    float lnK1[2], K3[2], lnK3[2], K5[2];   // ADK constants of the two ionization stages
+    float inv_E_c;   // 1 / E_c
+    float l2K1[2], l2K3[2], K5[2], K3l2e[2];  // ADK: log2 K1, log2 K3, K5, K3 log2(e) / 3
     float Kon;       // deltat / T0
-    float ve_c;      // drift velocity = F * ve_c
-    float K3c;       // sigma_coll * rho_nt
+    float Kuv;       // sigma_coll rho_nt v_e per unit F (v_e = e E0 / (sqrt 2 me w0))
     float K4w0;      // k0 w0^2 / (n0 rho_c)
     float w0sq;      // w0^2
     float inv_w0;    // 1 / w0
-    float inv_I1;    // 1 / I1 (I1 in eV, as the reference divides by it)
+    float invI1_Kon; // Kon / I1 (I1 in eV, as the reference divides by it)
     float rho_half;  // rho_nt / 2
     int plasma;      // 1 = ionization and plasma terms on
 };
@@ -52,7 +58,7 @@ struct NLConst {
 template <int NT, int P>
 struct PencilView {
     static constexpr int NLINES = P;
-    static __device__ __forceinline__ int at(int pos, int p) {
+    static constexpr __host__ __device__ __forceinline__ int at(int pos, int p) {
         if constexpr (P < 16) return pos * P + p + P * ((pos >> 4) + (pos >> 5));
         else return pos * P + p;
     }
@@ -73,7 +79,7 @@ struct PencilArgs {
     const void* in;          // input field (layout by mode)
     void* out;               // output field (may alias in)
     float2* scratch;         // per-CTA dA scratch, gridDim.x * Nt * P complex64
-    const float2* tw;        // W_Nt table
+    const float4* tw;        // W_Nt table {c, s, -eps, 0}
     const float* wpos;       // omega of each t position (FFT position order), Nt
     double* pencil_energy;   // EXIT: sum_t |out|^2 per pencil, Nx*Ny
     double* temp;            // TEMP: sum_xy |out|^2 per t, Nt (accumulated)
@@ -169,45 +175,80 @@ __device__ __forceinline__ void scan_chunks(M* maps, int tid) {
     }
 }
 
-// Per-point ionization inputs of one sample (plasma.c:133-213 in FP32, the A18 fix applied).
+// Small-argument elementary functions, from their Taylor series (|x| below the stated bound;
+// the CUDA library function is called outside it).  Per split step the nonlinear phase is
+// < 0.25 rad and the amplitude exponent < 1/64, so the series branch is the one taken.
+// 1 - exp(-x), x >= 0: alternating series to x^6/720 (relative truncation < x^6/5040 < 8e-10)
+__device__ __forceinline__ float one_minus_exp_neg(float x) {
+    if (x < 0.125f)
+        return x * (1.0f - x * (0.5f - x * (1.0f / 6.0f - x * (1.0f / 24.0f - x * (1.0f / 120.0f - x * (1.0f / 720.0f))))));
+    return 1.0f - expf(-x);
+}
+// exp(x): series to x^4/24 for |x| < 1/64 (truncation < |x|^5/120 < 1e-11)
+__device__ __forceinline__ float exp_small(float x) {
+    if (fabsf(x) < 0.015625f) return 1.0f + x * (1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f))));
+    return expf(x);
+}
+// sin and cos: series to x^7/7! and x^8/8! for |x| < 1/4 (truncation < 3e-11)
+__device__ __forceinline__ void sincos_small(float x, float* sn, float* cs) {
+    if (fabsf(x) < 0.25f) {
+        const float x2 = x * x;
+        *sn = x * (1.0f - x2 * (1.0f / 6.0f - x2 * (1.0f / 120.0f - x2 * (1.0f / 5040.0f))));
+        *cs = 1.0f - x2 * (0.5f - x2 * (1.0f / 24.0f - x2 * (1.0f / 720.0f - x2 * (1.0f / 40320.0f))));
+    } else {
+        sincosf(x, sn, cs);
+    }
+}
+
+// Per-point ionization coefficients of one sample (plasma.c:133-213 in FP32, A18 fix
+// applied).  The ADK rates are evaluated in the log2 domain:
+//   log2 W = log2 K1 + K5 (log2 K3 - log2 F) - K3 / (3 F ln 2).
+// Second-stage probabilities c2 below 2^-60 per slice are flushed to zero: their whole-pencil
+// effect on ions2 is < Nt 2^-60 < 2e-15, far below FP32 resolution, and a tile without any
+// second-stage ionization then skips the (ions2, ions1) scan, which is exact there.
 struct IonPoint {
-    float a, b, c2;  // scan coefficients
-    float qw;        // K4 w0 / (u^2 + w0^2) = sigma * w0 * tau_c (defocusing weight)
-    float sigma;     // K4 tau_c / (1 + w0^2 tau_c^2), tau_c = 1/u
+    float a, b, c2;  // scan coefficients W1 Kon, Wava Kon, W2 Kon
+    float qw;        // sigma w0 tau_c = K4 w0 / (u^2 + w0^2) (defocusing weight)
+    float sigma;     // K4 tau_c / (1 + w0^2 tau_c^2)
     float u;         // 1 / tau_c = sigma_coll rho_nt v_e
-    float I;
 };
 __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
     IonPoint r;
-    float I = (a.x * a.x + a.y * a.y) * c.I_scale;
-    if (I == 0.0f) I = 1e-30f;
-    const float F = sqrtf(I) * c.E_c;
-    const float lnF = logf(F);
-    const float invF = 1.0f / F;
+    float I = fmaf(a.x, a.x, a.y * a.y) * c.I_scale;
+    if (I == 0.0f) I = 1e-30f;                   // plasma.c:136-138
+    const float rs = rsqrtf(I);
+    const float F = I * rs * c.E_c;              // |E| in atomic units
+    const float invF = rs * c.inv_E_c;
+    const float l2F = __log2f(F);
     float w[2];
 #pragma unroll
-    for (int s = 0; s < 2; s++) {
-        const float ex = c.K3[s] * invF * (1.0f / 3.0f);
-        w[s] = (ex < 100.0f) ? expf(c.lnK1[s] + c.K5[s] * (c.lnK3[s] - lnF) - ex) : 0.0f;
+    for (int st = 0; st < 2; st++) {
+        const float e2 = c.l2K1[st] + c.K5[st] * (c.l2K3[st] - l2F) - c.K3l2e[st] * invF;
+        w[st] = (e2 > -126.0f) ? exp2f(e2) : 0.0f;
     }
-    const float u = c.K3c * (F * c.ve_c);      // 1 / tau_c
-    const float qw = c.K4w0 / fmaf(u, u, c.w0sq);
-    const float sigma = qw * u * c.inv_w0;
-    const float wava = sigma * I * c.inv_I1;
-    r.a = w[0] * c.Kon;
-    r.b = wava * c.Kon;
-    r.c2 = w[1] * c.Kon;
+    const float u = c.Kuv * F;
+    const float qw = __fdividef(c.K4w0, fmaf(u, u, c.w0sq));
+    r.sigma = qw * u * c.inv_w0;
     r.qw = qw;
-    r.sigma = sigma;
     r.u = u;
-    r.I = I;
+    r.a = w[0] * c.Kon;
+    r.b = r.sigma * I * c.invI1_Kon;
+    const float c2 = w[1] * c.Kon;
+    r.c2 = (c2 >= 8.673617e-19f) ? c2 : 0.0f;
     return r;
 }
 
 // Nonlinear step on a tile holding A(t) of P pencils in shared memory (natural t order).
 // IONIZ_ONLY = false: A *= exp(dz * A_nl) in place (propagation.c:244-327 with the A13/A14
 // fixes).  IONIZ_ONLY = true: write tau_c and freeelectrons_sp (plasma.c:118-245 outputs)
-// in the reference layout instead, A untouched.
+// in the reference layout instead, A untouched.  Thread (p = tid % P, ch = tid / P) walks
+// the 32 samples t = 32 ch .. 32 ch + 31 of pencil p.
+// Offset of sample t0 + i from sample t0 (t0 a multiple of 32, i < 32) in the pencil view.
+template <int P>
+__host__ __device__ __forceinline__ constexpr int walk_off(int i) {
+    return i * P + ((P < 16) ? P * (i >> 4) : 0);
+}
+
 template <int NT, int P, bool IONIZ_ONLY>
 __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restrict__ scr, const NLConst& c,
                                                void* scan_mem, int tid, double* tau_out, double* fe_out,
@@ -215,99 +256,105 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
     using V = PencilView<NT, P>;
     constexpr int TPP = NT / 32;
     const int p = tid % P;
-    const int ch = tid / P;       // chunk index within the pencil
+    const int ch = tid / P;
     const int t0 = ch * 32;
+    float2* w = s + V::at(t0, p);   // this thread's 32 samples: w[walk_off<P>(i)]
+    const float2* dA = scr + t0 * P + p;   // dA of the same samples: dA[i * P]
     if (c.plasma) {
         MapR* mr = reinterpret_cast<MapR*>(scan_mem);
         MapUV* muv = reinterpret_cast<MapUV*>(scan_mem);
-        // S1: chunk maps of the R recurrence
+        // S1: chunk map of the R recurrence (FP32 within the chunk)
+        int any2 = 0;
         {
             float B = 0.0f, C = 0.0f;
+#pragma unroll 8
             for (int i = 0; i < 32; i++) {
-                const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
+                const IonPoint ip = ion_point(w[walk_off<P>(i)], c);
                 const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
                 C = fmaf(1.0f - ip.b, C, Ck);
-                B = B + ip.b - B * ip.b;
+                B = fmaf(-B, ip.b, B + ip.b);
+                any2 |= (ip.c2 > 0.0f);
             }
             mr[p * TPP + ch] = MapR{(double)B, (double)C};
         }
-        __syncthreads();
-        scan_chunks<MapR, P, TPP>(mr, tid);
+        any2 = __syncthreads_or(any2);
+        scan_chunks<MapR, P, TPP>(mr, tid);   // carries across chunks in FP64
         __syncthreads();
         const float Rin = (float)mr[p * TPP + ch].C;
-        __syncthreads();
-        // S2: chunk maps of the (ions2, ions1) recurrence
-        {
+        float u = 0.0f, v = (Rin > 0.0f) ? one_minus_exp_neg(Rin) : 0.0f;
+        if (any2) {
+            __syncthreads();
+            // S2: chunk map of the (ions2, ions1) recurrence
             float R = Rin;
             float m00 = 1.f, m01 = 0.f, m10 = 0.f, m11 = 1.f, o0 = 0.f, o1 = 0.f;
+#pragma unroll 4
             for (int i = 0; i < 32; i++) {
                 const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
                 R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
-                const float g = -expm1f(-R);
+                const float g = one_minus_exp_neg(R);
                 const float n00 = fmaf(ip.c2, m10, m00), n01 = fmaf(ip.c2, m11, m01);
                 const float no0 = fmaf(ip.c2, o1, o0), no1 = g - o0;
-                m10 = -m00; m11 = -m01; m00 = n00; m01 = n01;
-                o1 = no1; o0 = no0;
+                m10 = -m00;
+                m11 = -m01;
+                m00 = n00;
+                m01 = n01;
+                o1 = no1;
+                o0 = no0;
             }
             muv[p * TPP + ch] = MapUV{m00, m01, m10, m11, o0, o1};
+            __syncthreads();
+            scan_chunks<MapUV, P, TPP>(muv, tid);
+            __syncthreads();
+            u = (float)muv[p * TPP + ch].o0;
+            v = (float)muv[p * TPP + ch].o1;
         }
-        __syncthreads();
-        scan_chunks<MapUV, P, TPP>(muv, tid);
-        __syncthreads();
-        float u = (float)muv[p * TPP + ch].o0;
-        float v = (float)muv[p * TPP + ch].o1;
-        __syncthreads();
-        // S3: apply the nonlinear step
+        // S3: apply the nonlinear step (or emit the ionization outputs)
         float R = Rin;
+#pragma unroll 4
         for (int i = 0; i < 32; i++) {
             const int t = t0 + i;
-            const float2 a = s[V::at(t, p)];
+            const float2 a = w[walk_off<P>(i)];
             const IonPoint ip = ion_point(a, c);
             R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
-            const float g = -expm1f(-R);
-            const float ions = fmaf(2.0f, u, v);
+            const float g = one_minus_exp_neg(R);
+            const float ions = fmaf(2.0f, u, v);     // state before slice t (plasma.c:238-241)
+            const float nu = fmaf(ip.c2, v, u);
+            v = g - u;
+            u = nu;
             if constexpr (IONIZ_ONLY) {
                 const size_t gi = (size_t)t * NP + q0 + p;
                 tau_out[gi] = 1.0 / (double)ip.u;
                 fe_out[gi] = (double)ions * (double)ip.sigma;
-                const float nu = fmaf(ip.c2, v, u);
-                v = g - u;
-                u = nu;
                 continue;
             }
             const float pl = c.rho_half * ions;
             float re = -pl * ip.sigma;
-            float im = c.gam * (a.x * a.x + a.y * a.y) - pl * ip.qw;
+            float im = fmaf(c.gam, fmaf(a.x, a.x, a.y * a.y), -pl * ip.qw);
             if (c.sst_c != 0.0f) {
-                const float2 d = scr[t * P + p];
-                const float2 sd = cmulc(d, a);  // d * conj(a)
+                const float2 sd = cmulc(dA[i * P], a);  // dA * conj(A)
                 re = fmaf(-3.0f * c.sst_c, sd.x, re);
                 im = fmaf(-c.sst_c, sd.y, im);
             }
-            const float nu = fmaf(ip.c2, v, u);
-            v = g - u;
-            u = nu;
-            const float amp = expf(c.dz * re);
+            const float amp = exp_small(c.dz * re);
             float sn, cs;
-            sincosf(c.dz * im, &sn, &cs);
-            s[V::at(t, p)] = cmul(a, make_float2(amp * cs, amp * sn));
+            sincos_small(c.dz * im, &sn, &cs);
+            w[walk_off<P>(i)] = cmul(a, make_float2(amp * cs, amp * sn));
         }
     } else {
+#pragma unroll 4
         for (int i = 0; i < 32; i++) {
-            const int t = t0 + i;
-            const float2 a = s[V::at(t, p)];
+            const float2 a = w[walk_off<P>(i)];
             float re = 0.0f;
-            float im = c.gam * (a.x * a.x + a.y * a.y);
+            float im = c.gam * fmaf(a.x, a.x, a.y * a.y);
             if (c.sst_c != 0.0f) {
-                const float2 d = scr[t * P + p];
-                const float2 sd = cmulc(d, a);
+                const float2 sd = cmulc(dA[i * P], a);
                 re = -3.0f * c.sst_c * sd.x;
                 im = fmaf(-c.sst_c, sd.y, im);
             }
-            const float amp = expf(c.dz * re);
+            const float amp = exp_small(c.dz * re);
             float sn, cs;
-            sincosf(c.dz * im, &sn, &cs);
-            s[V::at(t, p)] = cmul(a, make_float2(amp * cs, amp * sn));
+            sincos_small(c.dz * im, &sn, &cs);
+            w[walk_off<P>(i)] = cmul(a, make_float2(amp * cs, amp * sn));
         }
     }
 }
@@ -322,11 +369,27 @@ struct PencilCfg {
     static constexpr int SMEM_FIELD = View::SIZE * 8;  // bytes
     static constexpr int SMEM_SCAN = P * TPP * (int)sizeof(MapUV);
     static constexpr int SMEM_TEMP = NT * 8;            // FP64 temporal sums (TEMP mode)
-    static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TEMP;
+    static constexpr int SMEM_TW = NT * 16;             // W_Nt twiddles
+    static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TEMP + SMEM_TW;
     static_assert(NT * P == kTilePoints, "tile must hold 16384 points");
     static_assert((P * SLO) % 2 == 0, "rows must be whole float4s");
 };
 
+// L2 prefetch of the P*SLO*8 = 128 B rows of a slot-layout tile (overlaps the next tile's
+// DRAM reads with this tile's compute; one bulk prefetch per row)
+template <int NT, int P, int SLO>
+__device__ __forceinline__ void prefetch_tile(const float2* g, int q0, int NP, int tid) {
+    constexpr int ROWS = NT / SLO;
+    constexpr int BYTES = P * SLO * 8;
+    for (int row = tid; row < ROWS; row += kThreads) {
+        const float2* a = g + ((size_t)row * NP + q0) * SLO;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "n"(BYTES) : "memory");
+    }
+}
+
+// Element order of the two complex values of a float4 row chunk.  For SLO = 2 the pair is
+// (pos 2r, pos 2r + 1) of one pencil; odd rows store them in the opposite order so that
+// the four rows a warp touches fall on both halves of the shared-memory banks.
 // load a slot-layout tile into shared memory, optionally multiplied by -i*omega(pos)
 template <int NT, int P, int SLO, bool DERIV>
 __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ g, const float* __restrict__ wpos,
@@ -348,8 +411,13 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
             e0 = cscale(mul_mi<false>(e0), w0);
             e1 = cscale(mul_mi<false>(e1), w1);
         }
-        s[V::at(pos0, p0)] = e0;
-        s[V::at(pos1, p1)] = e1;
+        if (SLO == 2 && (row & 1)) {
+            s[V::at(pos1, p1)] = e1;
+            s[V::at(pos0, p0)] = e0;
+        } else {
+            s[V::at(pos0, p0)] = e0;
+            s[V::at(pos1, p1)] = e1;
+        }
     }
 }
 
@@ -365,7 +433,14 @@ __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__
         int pos0, p0, pos1, p1;
         if constexpr (SLO == 2) { pos0 = 2 * row; pos1 = pos0 + 1; p0 = p1 = c; }
         else { pos0 = pos1 = row; p0 = 2 * c; p1 = p0 + 1; }
-        const float2 e0 = s[V::at(pos0, p0)], e1 = s[V::at(pos1, p1)];
+        float2 e0, e1;
+        if (SLO == 2 && (row & 1)) {
+            e1 = s[V::at(pos1, p1)];
+            e0 = s[V::at(pos0, p0)];
+        } else {
+            e0 = s[V::at(pos0, p0)];
+            e1 = s[V::at(pos1, p1)];
+        }
         g4[gi] = make_float4(e0.x, e0.y, e1.x, e1.y);
     }
 }
@@ -381,7 +456,9 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
     double* tsum = reinterpret_cast<double*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN);
     const int tid = threadIdx.x;
     const int NP = args.NP;
-    const float2* tw = args.tw;
+    float4* tw = reinterpret_cast<float4*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN + Cfg::SMEM_TEMP);
+    for (int k = tid; k < NT; k += kThreads) tw[k] = __ldg(&args.tw[k]);
+    __syncthreads();
 
     if constexpr (MODE == PM_TEMP) {
         for (int t = tid; t < NT; t += kThreads) tsum[t] = 0.0;
@@ -390,6 +467,11 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
 
     for (int tile = blockIdx.x; tile < args.ntiles; tile += gridDim.x) {
         const int q0 = tile * P;
+        if constexpr (kPrefetch && (MODE == PM_STEP || MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP)) {
+            const int nxt = tile + gridDim.x;
+            if (nxt < args.ntiles)
+                prefetch_tile<NT, P, SLO>(reinterpret_cast<const float2*>(args.in), nxt * P, NP, tid);
+        }
         if constexpr (MODE == PM_IONIZ) {
             for (int f = tid; f < NT * P; f += kThreads) {
                 const int t = f / P, p = f - (f / P) * P;
@@ -468,9 +550,10 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
             __syncthreads();
         } else {  // PM_STEP
             const NLConst& c = args.nl;
-            float2* scr = args.scratch + (size_t)blockIdx.x * NT * P;
             const float2* gin = reinterpret_cast<const float2*>(args.in);
-            // dA = IFFT_t(-i omega S): the time derivative term of the self-steepening
+            float2* scr = args.scratch + (size_t)blockIdx.x * NT * P;
+            // dA = IFFT_t(-i omega S): the time derivative of the self-steepening term, kept in
+            // this CTA's scratch tile [t][p] (L2-resident) until the nonlinear walk
             if (c.sst_c != 0.0f) {
                 load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
                 __syncthreads();
@@ -502,22 +585,26 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
 // ---------------------------------------------------------------------------------------
 // Plane pass
 // ---------------------------------------------------------------------------------------
+// Linear-step factors as double-float complex numbers (x, y = high parts, z, w = low parts,
+// split from FP64).  Rounded once to complex64 the same factor would be applied every step
+// with the same rounding error, which adds up coherently over thousands of steps; the
+// low parts remove that systematic error.
 struct PlaneTables {
-    const float2* Rx;   // Nx, x position order
-    const float2* Ry;   // Ny, y position order
-    const float2* D;    // Nt, slot position order, includes 1/(Nx Ny Nt)
+    const float4* Rx;   // Nx, x position order: exp(-i zd kx^2 / (2 k0))
+    const float4* RyD;  // Ny * Nt, [y position][slot position]: Ry(ky) D(omega) scale
 };
 
 struct PlaneArgs {
     const float2* in;
     float2* out;
-    const float2* twx;
-    const float2* twy;
+    const float4* twx;       // W_Nx table {c, s, -eps, 0}
+    const float4* twy;
     PlaneTables t1;      // first (or only) linear operator
     PlaneTables t2;      // second half after the mirror lens (lens != 0)
     const float2* lensx; // exp(-i k0 x^2 / roc), real x order
     const float2* lensy;
     int lens;            // 1: L(t1) -> lens -> L(t2)
+    int Nt;
     int NP;
     int nunits;          // number of cluster work units
 };
@@ -529,7 +616,7 @@ struct PlaneCfg {
     static constexpr int RS = CX + 1;    // padded row stride
     static constexpr int RSZ = PB * RY * RS;  // region (one partner block), complex64
     static constexpr int SIZE = CL * RSZ;
-    static constexpr int SMEM = SIZE * 8 + (NX + NY) * 8;
+    static constexpr int SMEM = SIZE * 8 + (NX + NY) * 16;
     static_assert(SLO == 1 || PB == SLO, "interleaved slots are processed together");
     static_assert((RSZ % 2) == 0, "regions are moved as float4");
 };
@@ -538,7 +625,7 @@ template <int NX, int NY, int CL, int PB, int SLO>
 struct RowView {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     static constexpr int NLINES = PB * C::RY;
-    static __device__ __forceinline__ int at(int x, int l) {
+    static constexpr __host__ __device__ __forceinline__ int at(int x, int l) {
         return (x / C::CX) * C::RSZ + l * C::RS + (x % C::CX);
     }
 };
@@ -546,7 +633,7 @@ template <int NX, int NY, int CL, int PB, int SLO>
 struct ColView {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     static constexpr int NLINES = PB * C::CX;
-    static __device__ __forceinline__ int at(int y, int l) {
+    static constexpr __host__ __device__ __forceinline__ int at(int y, int l) {
         const int pl = l / C::CX, xl = l - pl * C::CX;
         return (y / C::RY) * C::RSZ + (pl * C::RY + (y % C::RY)) * C::RS + xl;
     }
@@ -593,29 +680,28 @@ __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& c
 
 template <int NX, int NY, int CL, int PB, int SLO>
 __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, const PlaneTables& T, int rank, int unit,
-                                             float2* tabx, cg::cluster_group& cluster, int tid) {
+                                             const float4* twx, const float4* twy, cg::cluster_group& cluster,
+                                             int tid) {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
     using CV = ColView<NX, NY, CL, PB, SLO>;
-    dif_all<NX, NX, RV>(s, a.twx, tid, kThreads);
+    dif_all<NX, NX, RV>(s, twx, tid, kThreads);
     cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
-    dif_all<NY, NY, CV>(s, a.twy, tid, kThreads);
-    // multiply by Rx(px) Ry(py) D(slot)
+    dif_all<NY, NY, CV>(s, twy, tid, kThreads);
+    // multiply by Rx(px) and Ry(py) D(slot) (double-float factors)
     for (int e = tid; e < PB * NY * C::CX; e += kThreads) {
         const int xl = e % C::CX;
         const int r = e / C::CX;
         const int y = r % NY, pl = r / NY;
         const int px = rank * C::CX + xl;
         const int slot = (SLO == 1) ? unit * PB + pl : unit * SLO + pl;
-        const float2 f = cmul(cmul(__ldg(&T.Rx[px]), __ldg(&T.Ry[y])), __ldg(&T.D[slot]));
         const int idx = CV::at(y, pl * C::CX + xl);
-        s[idx] = cmul(s[idx], f);
+        s[idx] = cmul_df(cmul_df(s[idx], __ldg(&T.Rx[px])), __ldg(&T.RyD[(size_t)y * a.Nt + slot]));
     }
     __syncthreads();
-    dit_all<NY, NY, CV>(s, a.twy, tid, kThreads);
+    dit_all<NY, NY, CV>(s, twy, tid, kThreads);
     cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
-    dit_all<NX, NX, RV>(s, a.twx, tid, kThreads);
-    (void)tabx;
+    dit_all<NX, NX, RV>(s, twx, tid, kThreads);
 }
 
 template <int NX, int NY, int CL, int PB, int SLO>
@@ -624,12 +710,16 @@ __global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
     using RV = RowView<NX, NY, CL, PB, SLO>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
-    float2* tabx = reinterpret_cast<float2*>(smem_raw + C::SIZE * 8);
+    float4* twx = reinterpret_cast<float4*>(smem_raw + C::SIZE * 8);
+    float4* twy = twx + NX;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int tid = threadIdx.x;
     const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;
     const int NP = a.NP;
+    for (int k = tid; k < NX; k += kThreads) twx[k] = __ldg(&a.twx[k]);
+    for (int k = tid; k < NY; k += kThreads) twy[k] = __ldg(&a.twy[k]);
+    __syncthreads();
 
     for (int unit = cid; unit < a.nunits; unit += ncl) {
         // load this CTA's rows: y in [rank*RY, rank*RY + RY) of PB planes
@@ -654,7 +744,7 @@ __global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
             }
         }
         __syncthreads();
-        plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t1, rank, unit, tabx, cluster, tid);
+        plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t1, rank, unit, twx, twy, cluster, tid);
         if (a.lens) {
             // mirror lens in real (x, y): exp(-i k0 (x^2 + y^2)/roc) = lensx[x] * lensy[y]
             for (int e = tid; e < PB * C::RY * NX; e += kThreads) {
@@ -666,7 +756,7 @@ __global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
                 s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y])));
             }
             __syncthreads();
-            plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t2, rank, unit, tabx, cluster, tid);
+            plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t2, rank, unit, twx, twy, cluster, tid);
         }
         for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += kThreads) {
             const int c = f % F4_ROW;

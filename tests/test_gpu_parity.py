@@ -154,4 +154,11 @@ def test_energy_conservation_no_plasma(gpu_lib):
         e0 = prop.energy()
         prop.run_fixed(100)
         e1 = prop.energy()
-    assert abs(e1 / e0 - 1) < 2e-5
+    # the exponential integrator of the self-steepening term changes the energy at O(dz^2);
+    # the device run reproduces the FP64 oracle's own drift
+    ref = A.copy()
+    st = o.new_state()
+    o.run_fixed(ref, st, 100)
+    drift_ref = o.energy(ref) / o.energy(A) - 1
+    assert abs(drift_ref) < 5e-5
+    assert abs((e1 / e0 - 1) - drift_ref) < 1e-6

@@ -123,6 +123,72 @@ def test_position_frequency_table(N):
     assert sorted(closed) == list(range(N))
 
 
+SHAPES = [(16, 16, 64), (32, 32, 256), (64, 64, 512), (128, 128, 1024), (256, 256, 512), (256, 256, 2048),
+          (512, 512, 1024)]
+
+
+def _shape_cfg(NX, NY, NT):
+    """Tile and cluster parameters, as mpc_shapes.cuh derives them."""
+    P = 16384 // NT
+    SLO = 16 // P if P < 16 else 1
+    plane_b = NX * NY * 8
+    if SLO == 2:
+        CL, PB = plane_b * 2 // 131072, 2
+    elif plane_b > 131072:
+        CL, PB = plane_b // 131072, 1
+    else:
+        CL, PB = 1, min(131072 // plane_b, NT)
+    return P, SLO, CL, PB
+
+
+def _views(NX, NY, NT):
+    """Python statement of the shared-memory views of mpc_kernels.cuh:
+    (name, N, NLINES, at(pos, line), size)."""
+    P, SLO, CL, PB = _shape_cfg(NX, NY, NT)
+    if P < 16:
+        pen = lambda pos, l: pos * P + l + P * ((pos >> 4) + (pos >> 5))  # noqa: E731
+        psize = NT * P + P * (NT // 16 + NT // 32)
+    else:
+        pen = lambda pos, l: pos * P + l  # noqa: E731
+        psize = NT * P
+    CX, RY = NX // CL, NY // CL
+    RS = CX + 1
+    RSZ = PB * RY * RS
+    row = lambda x, l: (x // CX) * RSZ + l * RS + (x % CX)  # noqa: E731
+
+    def col(y, l):
+        pl, xl = divmod(l, CX)
+        return (y // RY) * RSZ + (pl * RY + (y % RY)) * RS + xl
+
+    return [("pencil", NT, P, pen, psize), ("row", NX, PB * RY, row, CL * RSZ), ("col", NY, PB * CX, col, CL * RSZ)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_fft_views_stage_separable_and_in_bounds(shape):
+    """The FFT stages address a butterfly as at(base) + at(S q) - at(0) (mpc_fft.cuh); check
+    that this equals at(base + S q) for every view, stage and butterfly, that every address
+    is inside the view's shared-memory buffer, and that the view is one-to-one."""
+    for name, N, NL, at, size in _views(*shape):
+        seen = set()
+        for pos in range(N):
+            for l in range(NL):
+                a = at(pos, l)
+                assert 0 <= a < size, (name, pos, l)
+                seen.add(a)
+        assert len(seen) == N * NL, name
+        L = N
+        while L > 1:
+            R = 16 if L >= 16 else L
+            S = L // R
+            for b in range(N // L):
+                for j in range(S):
+                    base = b * L + j
+                    for l in (0, 1, NL - 1):
+                        for q in range(R):
+                            assert at(base + S * q, l) == at(base, l) + at(S * q, 0) - at(0, 0), (name, L, b, j, l, q)
+            L //= R
+
+
 def _header_symbols():
     with open(os.path.join(ROOT, "include", "mpc_gpu.h")) as f:
         txt = f.read()
