@@ -6,7 +6,7 @@
  * argument meaning.  Differences, all deliberate:
  *   - the six FFT plan handles of createPlans become one opaque context (mpc_ctx);
  *   - every call returns an int status (MPC_OK = 0) and never exits the process;
- *   - the physics is the reference's with its defects corrected (the design doc lists each);
+ *   - the physics is the reference's with its numerical defects corrected;
  *   - a device-resident field API (mpc_field_*, mpc_run_*) avoids the per-step host copies
  *     the reference makes.
  * Field layout everywhere: A[k*Nx*Ny + j*Nx + i] (i = x fastest, k = t slowest), complex128

@@ -3,9 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY (the checker, and the timed CPU baseline).  Nothing in the
  * product path links or calls this file.  Each function cites the reference lines it
- * restates; where the reference is defective the defect number (A<n>, table in
- * the design doc) names the switch in or_switches that selects corrected (1) or as-written (0)
- * arithmetic.  The FFT is this file's own iterative radix-2 (the reference used FFTW
+ * restates; where the reference is defective a defect number A<n> in the comments names
+ * the switch in or_switches that selects corrected (1) or as-written (0) arithmetic.  The FFT is this file's own iterative radix-2 (the reference used FFTW
  * guru plans, propagation.c:554-603, which are not available here); it is checked
  * against numpy.fft by tests/test_oracle.py.
  */

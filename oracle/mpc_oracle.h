@@ -6,7 +6,7 @@
  * (mpc_gb300/, include/mpc_gpu.h) never links, imports or runs it.
  *
  * Parity status: the reference ships no tests, fixtures or golden vectors, and its
- * full propagator cannot be built (see the defect table in the design doc).  The pieces
+ * full propagator cannot be built (invalid Makefile, FFTW and MPI absent).  The pieces
  * of plasma.c / propagation.c that compile on their own (ADK, ionizpot, Natoms,
  * ioniz as written, calcexpR as written, calc1oes, setStep) are compiled from the
  * reference sources into oracle/_ref by oracle/build_ref.sh and pin this file's
@@ -45,7 +45,7 @@ typedef struct {
 } or_params;
 
 /* One switch per reference defect that changes numbers.  1 = corrected (default),
- * 0 = as written.  Numbers refer to the defect table in the design doc. */
+ * 0 = as written.  A<n> numbers the defect; the comment states it. */
 typedef struct {
     int diffr_phase;    /* A12: i restored in the diffraction exponent (propagation.c:386-389) */
     int diffr_fftorder; /* A12: diffraction table reordered to FFT order */
