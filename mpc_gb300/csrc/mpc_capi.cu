@@ -500,8 +500,11 @@ int mpc_destroy(mpc_ctx* c) {
     prof_clear(c);
     for (auto& kv : c->tables) cudaFree(kv.second.f64);
     if (c->ident.f64) cudaFree(c->ident.f64);
-    void* ptrs[] = {c->S, c->scratch, c->io, c->io2, c->twx, c->twy, c->twt, c->wpos, c->dfx, c->dfy,
-                    c->dft, c->dwr, c->dbetas, c->dr, c->lensx, c->lensy, c->penergy, c->dred};
+    // only the base of each allocation: dfy/dft, dbetas/dr and lensy point inside dfx, dwr
+    // and lensx, and cudaFree of an interior pointer fails and leaves an error pending in the
+    // (process-wide) runtime for the caller's next CUDA call
+    void* ptrs[] = {c->S,   c->scratch, c->io,  c->io2,     c->twx,    c->twy,  c->twt,
+                    c->wpos, c->dfx,    c->dwr, c->lensx,   c->penergy, c->dred};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->st) cudaStreamDestroy(c->st);

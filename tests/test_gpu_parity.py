@@ -162,3 +162,19 @@ def test_energy_conservation_no_plasma(gpu_lib):
     drift_ref = o.energy(ref) / o.energy(A) - 1
     assert abs(drift_ref) < 5e-5
     assert abs((e1 / e0 - 1) - drift_ref) < 1e-6
+
+
+def test_create_destroy_leaves_no_pending_error(gpu_lib):
+    """The library shares the CUDA runtime (libcudart.so) with its caller, so a failed runtime
+    call inside it would surface in the caller's next CUDA call; a context's whole life must
+    leave no error pending."""
+    import ctypes
+
+    from mpc_gb300.capi import Propagator
+    cudart = ctypes.CDLL("libcudart.so.13")      # the instance the library already loaded
+    cudart.cudaGetLastError.restype = ctypes.c_int
+    cudart.cudaGetLastError()
+    p, A = inputs.make_cell(inputs.config1(Nx=32, Ny=32, Nt=256))
+    with Propagator(p) as prop:
+        prop.ssfmprop(A.copy(), p.dzz, 1, 0.0, p.puls_e, change=1)
+    assert cudart.cudaGetLastError() == 0
