@@ -146,6 +146,31 @@ long mpc_launch_count(mpc_ctx *ctx);
 int mpc_profile(mpc_ctx *ctx, int on);
 int mpc_kernel_times(mpc_ctx *ctx, double *pencil_ms, long *n_pencil, double *plane_ms, long *n_plane);
 
+/* ---- allocation-free nonlinear step (no counterpart in the reference) -------------- */
+/* The nonlinear half of a split step, A *= exp(dz * A_nl(A)) with Kerr, self-steepening,
+ * ionization and plasma terms, applied in place to a field the caller already holds in
+ * device memory: complex64, real space, layout A[t*Nx*Ny + y*Nx + x], physical units,
+ * physics parameters from p (only dims, w, gamma2, w0, sst_on, plasm, deltat, rho_c,
+ * rho_nt, n0 and gas are read).
+ *
+ * For callers that cannot allocate device memory -- code running where cudaMalloc is not
+ * allowed or not safe (inside a host callback, or under another library's promise not to
+ * allocate), processes whose device memory is owned entirely by a pool handed out at
+ * start-up, hosts with a fixed device-memory budget -- this call allocates nothing: no
+ * cudaMalloc, no cudaFree, no context.  Its work buffers are one static device array of
+ * 8,445,952 bytes inside libmpc_gpu.so, which every GPU that loads the library holds
+ * until the process exits.  Limits: Nt one of 64, 256, 512, 1024, 2048 (at most 2048),
+ * Nx*Ny a multiple of 16384/Nt; larger or other sizes are rejected with MPC_ERR_SHAPE.
+ *
+ * The first call on a device looks up the device address of that array (and sets the
+ * kernel's shared-memory limit) with that device current; make the first call before any
+ * stream capture.  Every call shares the array and leaves its contents behind; nothing in
+ * it needs to start at zero (each call rewrites what it reads).  Calls that overlap on the
+ * GPU -- on different streams, or from several host threads -- race on the array.  The
+ * work is queued on `stream` (a cudaStream_t, NULL for the legacy stream) and the call
+ * returns without waiting; errors are printed to stderr and returned as MPC_ERR_*. */
+int mpc_nonlinear_noalloc(const mpc_params *p, void *A_dev, double dz, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,7 @@ SIGNATURES = {
     "mpc_launch_count": (C.c_long, [C.c_void_p]),
     "mpc_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_kernel_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long), _dp, C.POINTER(C.c_long)]),
+    "mpc_nonlinear_noalloc": (C.c_int, [C.POINTER(c_mpc_params), C.c_void_p, C.c_double, C.c_void_p]),
 }
 
 _lib = None
@@ -292,3 +293,19 @@ def calc1oes(BP: np.ndarray, r: np.ndarray):
     y = np.zeros(4)
     _check(lib.mpc_calc1oes(_ptr(BP), BP.size, _ptr(r), C.byref(v), _ptr(y)), "mpc_calc1oes")
     return v.value, y
+
+
+def nonlinear_noalloc(p: MPCParams, A_dev_ptr: int, dz: float, stream: int = 0) -> int:
+    """Apply the nonlinear step in place to a complex64 field already in device memory
+    (address A_dev_ptr, real space, reference layout, physical units) without allocating
+    device memory: for callers that cannot call cudaMalloc.  The work is queued on `stream`
+    (a cudaStream_t as an integer); returns the MPC status code."""
+    lib = load()
+    keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (p.betas, p.wr, p.w, p.r)]
+    cp = c_mpc_params()
+    cp.dims[:] = list(p.dims)
+    cp.betas, cp.wr, cp.w, cp.r = (_ptr(x) for x in keep)
+    cp.sst_on, cp.gamma2, cp.w0, cp.plasm = p.sst_on, p.gamma2, p.w0, p.plasm
+    cp.deltat, cp.rho_c, cp.rho_nt, cp.n0 = p.deltat, p.rho_c, p.rho_nt, p.n0
+    cp.gas = p.gas.encode("ascii")[:8]
+    return int(lib.mpc_nonlinear_noalloc(C.byref(cp), C.c_void_p(A_dev_ptr), dz, C.c_void_p(stream)))
