@@ -247,10 +247,10 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        nst = 1
+        nst = 5  # about 10 s on 16 host cores
         dt = cpu_baseline_run(p, A, nst, cores)
         cpu = {"value": p.N * nst / dt, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{nst} split step of the 256x256x2048 cell, FP64 oracle/ restatement, OpenMP"}
+               "sample": f"{nst} split steps of the 256x256x2048 cell, FP64 oracle/ restatement, OpenMP"}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -268,6 +268,19 @@ def run_gb300(args):
         dist.barrier()
 
 
+def run_profile_case(nsteps: int):
+    """A short target for ncu: upload the workload's field and run `nsteps` split steps,
+    with no timing.  Launch order: the entry pencil sweep (template mode 0), then per split
+    step one pencil sweep (mode 2) and one plane sweep."""
+    from mpc_gb300 import capi
+    cfg, p, A = make_workload()
+    with capi.Propagator(p) as prop:
+        prop.upload(A, calibrate=True)
+        prop.run_fixed(nsteps)
+        prop.sync()
+        print(json.dumps({"profile_case": nsteps, "grid": [p.Nx, p.Ny, p.Nt], "launches": prop.launch_count()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -275,8 +288,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="NSTEPS",
+                    help="run NSTEPS split steps of the workload and exit (an ncu target)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)
