@@ -177,7 +177,8 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     from mpc_gb300 import capi
     cfg, p, A = make_workload()
-    prop = capi.Propagator(p)
+    prop = capi.Propagator(p.copy(variant=-1))   # the autotuner picks the kernel variant
+    vinfo = prop.variant_info()
     # pinned host field for the end-to-end path (physical units, calibrated)
     pin = capi.PinnedArray(p.N)
     pin.array[:] = A
@@ -259,7 +260,7 @@ def run_gb300(args):
                 "config": {"workload": "multipass cell 256x256x2048, 400 fixed split steps per pass (1 pass = 1 step), "
                                        "lens mirror, SST + ADK + plasma on", "grid": [p.Nx, p.Ny, p.Nt],
                            "split_steps_per_step": STEPS_PER_PASS, "l2": "field 1 GiB > L2, no flush",
-                           "parallelism": f"replicas x{world}"},
+                           "parallelism": f"replicas x{world}", "kernel_variant": vinfo},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
     prop.close()

@@ -53,6 +53,9 @@ typedef struct {
     char gas[9];
     int bounce_mode;        /* MPC_BOUNCE_SIGNFLIP (reference) or MPC_BOUNCE_LENS */
     double roc;             /* mirror radius of curvature [m], lens mode */
+    int variant;            /* compiled kernel variant of this grid (layout and launch shapes; all
+                               give the same results): 0 = default, k = the k-th, -1 = the
+                               fastest, timed when the context is created */
 } mpc_params;
 
 typedef struct mpc_ctx mpc_ctx;
@@ -141,6 +144,11 @@ int mpc_host_free(void *ptr);
 int mpc_stream_handle(mpc_ctx *ctx, void **stream);
 /* Number of kernels this context has launched so far. */
 long mpc_launch_count(mpc_ctx *ctx);
+/* The compiled kernel variant this context runs (the autotuner's pick when created with
+ * variant = -1) and its launch shapes: info = {P pencils per tile, SLO slots interleaved,
+ * CL CTAs per plane cluster, PB planes per cluster unit, PT plane threads per CTA,
+ * pencil CTAs launched, plane clusters launched, pencil threads per CTA}. */
+int mpc_variant_info(mpc_ctx *ctx, int *variant, int info[8]);
 /* With on != 0, every pencil and plane sweep is bracketed by CUDA events on the context's
  * stream; mpc_kernel_times sums their durations since the last enable (synchronises). */
 int mpc_profile(mpc_ctx *ctx, int on);

@@ -31,7 +31,8 @@ class c_mpc_params(C.Structure):
                 ("plasm", C.c_int), ("deltat", C.c_double), ("rho_c", C.c_double), ("rho_nt", C.c_double),
                 ("n0", C.c_double), ("puls_e", C.c_double), ("Ab_M", C.c_double), ("r", _dp),
                 ("dr", C.c_double), ("def_err", C.c_double), ("dzmin", C.c_double), ("Esig", C.c_double),
-                ("gas", C.c_char * 9), ("bounce_mode", C.c_int), ("roc", C.c_double)]
+                ("gas", C.c_char * 9), ("bounce_mode", C.c_int), ("roc", C.c_double),
+                ("variant", C.c_int)]
 
 
 class c_mpc_state(C.Structure):
@@ -67,6 +68,7 @@ SIGNATURES = {
     "mpc_host_free": (C.c_int, [C.c_void_p]),
     "mpc_stream_handle": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "mpc_launch_count": (C.c_long, [C.c_void_p]),
+    "mpc_variant_info": (C.c_int, [C.c_void_p, _ip, _ip]),
     "mpc_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_kernel_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long), _dp, C.POINTER(C.c_long)]),
     "mpc_nonlinear_noalloc": (C.c_int, [C.POINTER(c_mpc_params), C.c_void_p, C.c_double, C.c_void_p]),
@@ -127,6 +129,7 @@ class Propagator:
         cp.puls_e, cp.Ab_M, cp.dr, cp.def_err, cp.dzmin, cp.Esig = p.puls_e, p.Ab_M, p.dr, p.def_err, p.dzmin, p.Esig
         cp.gas = p.gas.encode("ascii")[:8]
         cp.bounce_mode, cp.roc = p.bounce_mode, p.roc
+        cp.variant = p.variant
         self._cp = cp
         h = C.c_void_p()
         _check(self.lib.mpc_create(C.byref(h), C.byref(cp)), "mpc_create")
@@ -242,6 +245,14 @@ class Propagator:
 
     def sync(self) -> None:
         _check(self.lib.mpc_sync(self.h), "mpc_sync")
+
+    def variant_info(self) -> dict:
+        """The kernel variant this context runs and its launch shapes."""
+        v = C.c_int(0)
+        info = (C.c_int * 8)()
+        _check(self.lib.mpc_variant_info(self.h, C.byref(v), info), "mpc_variant_info")
+        keys = ("P", "SLO", "CL", "PB", "PT", "pencil_ctas", "plane_clusters", "pencil_threads")
+        return dict(variant=v.value, **dict(zip(keys, list(info))))
 
     def launch_count(self) -> int:
         return int(self.lib.mpc_launch_count(self.h))

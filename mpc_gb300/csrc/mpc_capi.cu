@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -216,6 +217,7 @@ struct TableSet {
 
 struct mpc_ctx {
     const ShapeOps* ops = nullptr;
+    int variant = 0;    // index of ops among the compiled variants of the grid
     int Nx = 0, Ny = 0, Nt = 0;
     long NP = 0, N = 0;
     mpc_params p{};
@@ -232,7 +234,7 @@ struct mpc_ctx {
     float2* scratch = nullptr;
     double2* io = nullptr;      // complex128 staging, N
     double2* io2 = nullptr;     // second complex128 staging (setStep)
-    float4 *twx = nullptr, *twy = nullptr, *twt = nullptr;
+    float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;  // packed twiddle tables
     float* wpos = nullptr;
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
     std::vector<int> hfx, hfy, hft;
@@ -272,11 +274,13 @@ static void prof_clear(mpc_ctx* c) {
     c->events.clear();
 }
 
-static const ShapeOps* find_shape(int Nx, int Ny, int Nt) {
+// Compiled variant `variant` (0 = the first) of a grid shape, or null.
+static const ShapeOps* find_shape(int Nx, int Ny, int Nt, int variant = 0) {
     const ShapeOps* const* lists[] = {mpc::shape_list_a, mpc::shape_list_b, mpc::shape_list_c, mpc::shape_list_d};
+    int k = 0;
     for (auto l : lists)
         for (int i = 0; l[i]; i++)
-            if (l[i]->Nx == Nx && l[i]->Ny == Ny && l[i]->Nt == Nt) return l[i];
+            if (l[i]->Nx == Nx && l[i]->Ny == Ny && l[i]->Nt == Nt && k++ == variant) return l[i];
     return nullptr;
 }
 
@@ -304,17 +308,20 @@ static std::vector<int> freq_of_pos(int N) {
     return f;
 }
 
-// W_N^k rounded to FP32 from FP64, plus -(|W|^2 - 1) of the rounded value (see mpc_fft.cuh)
-static int upload_twiddles(int N, float4** d) {
-    std::vector<float4> h(N);
+// Packed W_N table (mpc_fft.cuh Twiddles): N float2 W_N^k rounded to FP32 from FP64, then N
+// float -(|W|^2 - 1) of the rounded values
+static int upload_twiddles(int N, float2** d) {
+    std::vector<float> h(3 * (size_t)N);
     for (int k = 0; k < N; k++) {
         const double a = -2.0 * M_PI * (double)k / (double)N;
         const float c = (float)cos(a), s = (float)sin(a);
         const double eps = (double)c * c + (double)s * s - 1.0;
-        h[k] = make_float4(c, s, (float)-eps, 0.0f);
+        h[2 * k] = c;
+        h[2 * k + 1] = s;
+        h[2 * (size_t)N + k] = (float)-eps;
     }
-    CK(cudaMalloc(d, sizeof(float4) * N), "cudaMalloc twiddles");
-    CK(cudaMemcpy(*d, h.data(), sizeof(float4) * N, cudaMemcpyHostToDevice), "copy twiddles");
+    CK(cudaMalloc(d, mpc::twiddle_bytes(N)), "cudaMalloc twiddles");
+    CK(cudaMemcpy(*d, h.data(), mpc::twiddle_bytes(N), cudaMemcpyHostToDevice), "copy twiddles");
     return MPC_OK;
 }
 
@@ -512,17 +519,28 @@ int mpc_destroy(mpc_ctx* c) {
     return MPC_OK;
 }
 
+static int autotune_variant(const mpc_params* p, int* best);
+
 int mpc_create(mpc_ctx** out, const mpc_params* p) {
     if (!out || !p) return fail(MPC_ERR_ARG, "null argument");
     *out = nullptr;
     const int Nx = p->dims[0], Ny = p->dims[1], Nt = p->dims[2];
     if (Nx != Ny) return fail(MPC_ERR_SHAPE, "the k grid wr of param.bin serves both x and y: Nx must equal Ny");
-    const ShapeOps* ops = find_shape(Nx, Ny, Nt);
-    if (!ops) return fail(MPC_ERR_SHAPE, "grid shape not compiled into libmpc_gpu");
+    if (!find_shape(Nx, Ny, Nt)) return fail(MPC_ERR_SHAPE, "grid shape not compiled into libmpc_gpu");
+    if (p->variant < -1) return fail(MPC_ERR_ARG, "variant must be -1 (autotune) or a variant index");
+    if (p->variant == -1) {
+        mpc_params q = *p;
+        int rc = autotune_variant(p, &q.variant);
+        if (rc) return rc;
+        return mpc_create(out, &q);
+    }
+    const ShapeOps* ops = find_shape(Nx, Ny, Nt, p->variant > 0 ? p->variant : 0);
+    if (!ops) return fail(MPC_ERR_ARG, "no such kernel variant of this grid shape");
     if (!p->betas || !p->wr || !p->w || !p->r) return fail(MPC_ERR_ARG, "null parameter array");
     if (!(p->k0 > 0) || !(p->w0 > 0) || !(p->Cav > 0)) return fail(MPC_ERR_ARG, "k0, w0 and Cav must be positive");
     mpc_ctx* c = new mpc_ctx();
     c->ops = ops;
+    c->variant = p->variant > 0 ? p->variant : 0;
     c->Nx = Nx;
     c->Ny = Ny;
     c->Nt = Nt;
@@ -560,7 +578,12 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
     TRYC(ops->setup(), "kernel attribute setup");
     TRYC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
     const int ntiles = (int)(c->NP / ops->P);
-    c->pencil_grid = ntiles < c->nsm ? ntiles : c->nsm;
+    const int per_sm = ops->pencil_blocks_per_sm();
+    if (per_sm <= 0) {
+        mpc_destroy(c);
+        return fail(MPC_ERR_CUDA, "pencil sweep configuration cannot be scheduled on this device");
+    }
+    c->pencil_grid = ntiles < c->nsm * per_sm ? ntiles : c->nsm * per_sm;
     const int nunits = ops->SLO == 2 ? Nt / 2 : Nt / ops->PB;
     int mc = ops->max_clusters();
     if (mc <= 0) {
@@ -572,7 +595,7 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
         mpc_destroy(c);
         return fail(MPC_ERR_NOMEM, "cudaMalloc field");
     }
-    TRYC(cudaMalloc(&c->scratch, sizeof(float2) * (size_t)c->pencil_grid * mpc::kTilePoints), "cudaMalloc scratch");
+    TRYC(cudaMalloc(&c->scratch, sizeof(float2) * (size_t)c->pencil_grid * ops->P * Nt), "cudaMalloc scratch");
     TRY(upload_twiddles(Nx, &c->twx));
     TRY(upload_twiddles(Ny, &c->twy));
     TRY(upload_twiddles(Nt, &c->twt));
@@ -624,6 +647,72 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
 #undef TRY
 #undef TRYC
     *out = c;
+    return MPC_OK;
+}
+
+// The autotuner: the fastest compiled variant of a grid on the current device.  Each variant
+// (device layout, pencil tile, plane cluster shape and CTA size; all give identical results)
+// runs 2 + 3 split steps -- one pencil sweep and one plane sweep each -- on a zero field in a
+// context of its own, timed with CUDA events over the last 3.  The choice is cached per device
+// and grid for the life of the process.  The nonlinear step's cost depends on the field, but
+// the shapes compared here do not change that part.
+static int pencil_step(mpc_ctx* c, double dz);
+
+static int autotune_variant(const mpc_params* p, int* best) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int>, int> cache;
+    int dev = 0;
+    CK(cudaGetDevice(&dev), "cudaGetDevice");
+    const auto key = std::make_tuple(dev, p->dims[0], p->dims[1], p->dims[2]);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        *best = it->second;
+        return MPC_OK;
+    }
+    int nvar = 0;
+    while (find_shape(p->dims[0], p->dims[1], p->dims[2], nvar)) nvar++;
+    float best_ms = 0.0f;
+    *best = -1;
+    for (int v = 0; v < nvar; v++) {
+        mpc_params q = *p;
+        q.variant = v;
+        mpc_ctx* c = nullptr;
+        if (mpc_create(&c, &q) != MPC_OK) {  // e.g. a cluster shape this device cannot place
+            cudaGetLastError();                  // leave no error pending for the caller
+            continue;
+        }
+        float ms = -1.0f;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        bool ok = cudaMemsetAsync(c->S, 0, sizeof(float2) * c->N, c->st) == cudaSuccess &&
+                  cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+        TableSet t;
+        ok = ok && get_tables(c, q.dzz, q.dzz, 1.0 / ((double)c->NP * c->Nt), &t) == MPC_OK;
+        for (int i = 0; ok && i < 5; i++) {
+            if (i == 2) ok = cudaEventRecord(e0, c->st) == cudaSuccess;
+            ok = ok && pencil_step(c, q.dzz) == MPC_OK && launch_plane(c, c->S, c->S, t, nullptr) == MPC_OK;
+        }
+        ok = ok && cudaEventRecord(e1, c->st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        mpc_destroy(c);
+        if (ok && (*best < 0 || ms < best_ms)) {
+            *best = v;
+            best_ms = ms;
+        }
+    }
+    if (*best < 0) return fail(MPC_ERR_CUDA, "autotuner: no kernel variant of this grid ran on this device");
+    cache[key] = *best;
+    return MPC_OK;
+}
+
+int mpc_variant_info(mpc_ctx* c, int* variant, int* info) {
+    if (!c || !variant || !info) return fail(MPC_ERR_ARG, "null argument");
+    *variant = c->variant;
+    const int v[8] = {c->ops->P, c->ops->SLO, c->ops->CL, c->ops->PB, c->ops->PT, c->pencil_grid,
+                      c->plane_clusters, c->ops->P * c->Nt / 32};
+    for (int i = 0; i < 8; i++) info[i] = v[i];
     return MPC_OK;
 }
 

@@ -161,20 +161,34 @@ struct Radix {
 // ---- batched in-place stages over a shared-memory view --------------------------------
 // View: NLINES independent lines of length N; element `pos` of line `l` lives at
 // V::at(pos, l).  Work items are (line, butterfly) pairs, lines fastest across threads.
-// tw: twiddle table in shared memory, entry k = {c, s, -eps, 0} with (c, s) = W_N^k =
-// exp(-2 pi i k / N) rounded to FP32 from FP64 and eps = c^2 + s^2 - 1 (computed in FP64 from
-// the rounded values).  The forward (DIF) stage multiplies by (c, s); the inverse (DIT) stage
-// by conj(c, s) * (1 - eps), so every forward/inverse round trip has gain 1 - eps^2 per path
-// instead of 1 + eps: rounded twiddles alone lose ~6e-8 of the energy per split step.
+// tw: twiddle table of W_N, packed as N float2 w[k] = (c, s) = exp(-2 pi i k / N) rounded to
+// FP32 from FP64, followed by N float e[k] = -eps with eps = c^2 + s^2 - 1 (computed in FP64
+// from the rounded values).  The forward (DIF) stage multiplies by (c, s); the inverse (DIT)
+// stage by conj(c, s) * (1 - eps), so every forward/inverse round trip has gain 1 - eps^2 per
+// path instead of 1 + eps: rounded twiddles alone lose ~6e-8 of the energy per split step.
 //
 // Every view used here is "stage separable": for a butterfly of span S starting at
 // base = b*L + j (j < S), V::at(base + S*q, l) == V::at(base, l) + V::at(S*q, 0) - V::at(0, 0),
 // so the R addresses of a butterfly are one computed base plus compile-time offsets
 // (tests/test_host.py checks the property for every view and stage of the library).
 
+struct Twiddles {
+    const float2* w;  // N entries (c, s)
+    const float* e;   // N entries -eps
+    // a packed table of N entries starting at p (shared or global memory)
+    __host__ __device__ static Twiddles packed(const void* p, int N) {
+        Twiddles t;
+        t.w = static_cast<const float2*>(p);
+        t.e = reinterpret_cast<const float*>(t.w + N);
+        return t;
+    }
+};
+// bytes of a packed table of N entries
+__host__ __device__ constexpr int twiddle_bytes(int N) { return N * 12; }
+
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
 template <int N, int L, class V>
-__device__ __forceinline__ void dif_stage(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -189,12 +203,9 @@ __device__ __forceinline__ void dif_stage(float2* s, const float4* __restrict__ 
         for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         dft<R, false>(v);
         if (S > 1) {
-            const float4* t = tw + j * (N / L);
+            const float2* t = tw.w + j * (N / L);
 #pragma unroll
-            for (int k = 1; k < R; k++) {
-                const float4 w = t[j * (k - 1) * (N / L)];
-                v[k] = cmul(v[k], make_float2(w.x, w.y));
-            }
+            for (int k = 1; k < R; k++) v[k] = cmul(v[k], t[j * (k - 1) * (N / L)]);
         }
 #pragma unroll
         for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
@@ -203,7 +214,7 @@ __device__ __forceinline__ void dif_stage(float2* s, const float4* __restrict__ 
 
 // DIT stage (exact transpose of the DIF stage with conjugate twiddles).
 template <int N, int L, class V>
-__device__ __forceinline__ void dit_stage(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -217,12 +228,13 @@ __device__ __forceinline__ void dit_stage(float2* s, const float4* __restrict__ 
 #pragma unroll
         for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         if (S > 1) {
-            const float4* t = tw + j * (N / L);
+            const float2* t = tw.w + j * (N / L);
+            const float* te = tw.e + j * (N / L);
 #pragma unroll
             for (int k = 1; k < R; k++) {
-                const float4 w = t[j * (k - 1) * (N / L)];
-                const float2 u = cmulc(v[k], make_float2(w.x, w.y));
-                v[k] = make_float2(fmaf(u.x, w.z, u.x), fmaf(u.y, w.z, u.y));
+                const float2 u = cmulc(v[k], t[j * (k - 1) * (N / L)]);
+                const float e = te[j * (k - 1) * (N / L)];
+                v[k] = make_float2(fmaf(u.x, e, u.x), fmaf(u.y, e, u.y));
             }
         }
         dft<R, true>(v);
@@ -233,7 +245,7 @@ __device__ __forceinline__ void dit_stage(float2* s, const float4* __restrict__ 
 
 // Whole forward transform (natural -> position order).  Ends with a __syncthreads.
 template <int N, int L, class V>
-__device__ __forceinline__ void dif_all(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid, int nthr) {
     dif_stage<N, L, V>(s, tw, tid, nthr);
     __syncthreads();
     constexpr int R = Radix<L>::R;
@@ -242,7 +254,7 @@ __device__ __forceinline__ void dif_all(float2* s, const float4* __restrict__ tw
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
 template <int N, int L, class V>
-__device__ __forceinline__ void dit_all(float2* s, const float4* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     if constexpr (L / R > 1) dit_all<N, L / R, V>(s, tw, tid, nthr);
     dit_stage<N, L, V>(s, tw, tid, nthr);

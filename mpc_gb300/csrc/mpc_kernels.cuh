@@ -25,14 +25,14 @@ namespace cg = cooperative_groups;
 
 namespace mpc {
 
-constexpr int kThreads = 512;          // both sweeps
+constexpr int kThreads = 512;          // threads of a one-CTA-per-SM launch (128 registers each)
 // L2 prefetch of the next pencil tile: measured slower on GB300 (it evicts the dA scratch
 // tiles from L2), so off by default
 #ifndef MPC_PREFETCH
 #define MPC_PREFETCH 0
 #endif
 constexpr bool kPrefetch = MPC_PREFETCH != 0;
-constexpr int kTilePoints = 16384;     // pencil tile: P * Nt complex points (128 KB)
+constexpr int kTilePoints = 16384;     // default pencil tile: P * Nt complex points (128 KB)
 
 // FP32 constants of the nonlinear step, computed on the host in FP64.
 struct NLConst {
@@ -53,16 +53,22 @@ struct NLConst {
     int plasma;      // 1 = ionization and plasma terms on
 };
 
-// Pencil tile view: line = pencil p, element (pos, p).  For P < 16 a pad keeps the
-// span-1 FFT stages and the per-thread t walks free of shared-memory bank conflicts.
+// Pencil tile view: line = pencil p, element (pos, p).  For P < 16 a pad of P slots every
+// 2^SH positions and every 32 positions keeps the FFT stages and the per-thread t walks free
+// of shared-memory bank conflicts (SH = 4 for P = 8, 3 for P = 4).  The pad depends on pos
+// only through pos >> 3, >> 4 and >> 5, so a walk of 32 samples from a multiple of 32 has the
+// same offsets everywhere: at(t0 + i, p) - at(t0, p) == walk(i).
 template <int NT, int P>
 struct PencilView {
     static constexpr int NLINES = P;
+    static constexpr int SH = (P < 8) ? 3 : 4;
     static constexpr __host__ __device__ __forceinline__ int at(int pos, int p) {
-        if constexpr (P < 16) return pos * P + p + P * ((pos >> 4) + (pos >> 5));
+        if constexpr (P < 16) return pos * P + p + P * ((pos >> SH) + (pos >> 5));
         else return pos * P + p;
     }
-    static constexpr int SIZE = (P < 16) ? (NT * P + P * (NT / 16 + NT / 32)) : NT * P;
+    static constexpr __host__ __device__ __forceinline__ int walk(int i) { return at(i, 0) - at(0, 0); }
+    static constexpr int SIZE = (P < 16) ? (NT * P + P * ((NT >> SH) + NT / 32)) : NT * P;
+    static_assert(P >= 4, "pencil tile of at least 4 pencils");
 };
 
 enum PencilMode : int {
@@ -79,7 +85,7 @@ struct PencilArgs {
     const void* in;          // input field (layout by mode)
     void* out;               // output field (may alias in)
     float2* scratch;         // per-CTA dA scratch, gridDim.x * Nt * P complex64
-    const float4* tw;        // W_Nt table {c, s, -eps, 0}
+    const float2* tw;        // W_Nt table, packed (mpc_fft.cuh Twiddles)
     const float* wpos;       // omega of each t position (FFT position order), Nt
     double* pencil_energy;   // EXIT: sum_t |out|^2 per pencil, Nx*Ny
     double* temp;            // TEMP: sum_xy |out|^2 per t, Nt (accumulated)
@@ -145,7 +151,7 @@ __device__ __forceinline__ M shfl_up_map(const M& m, int off) {
 template <class M, int P, int TPP>
 __device__ __forceinline__ void scan_chunks(M* maps, int tid) {
     const int warp = tid >> 5, lane = tid & 31;
-    constexpr int NW = kThreads / 32;
+    constexpr int NW = P * TPP / 32;       // the CTA has one thread per 32-sample chunk
     constexpr int CPL = (TPP + 31) / 32;
     for (int p = warp; p < P; p += NW) {
         M* row = maps + p * TPP;
@@ -243,12 +249,6 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
 // fixes).  IONIZ_ONLY = true: write tau_c and freeelectrons_sp (plasma.c:118-245 outputs)
 // in the reference layout instead, A untouched.  Thread (p = tid % P, ch = tid / P) walks
 // the 32 samples t = 32 ch .. 32 ch + 31 of pencil p.
-// Offset of sample t0 + i from sample t0 (t0 a multiple of 32, i < 32) in the pencil view.
-template <int P>
-__host__ __device__ __forceinline__ constexpr int walk_off(int i) {
-    return i * P + ((P < 16) ? P * (i >> 4) : 0);
-}
-
 template <int NT, int P, bool IONIZ_ONLY>
 __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restrict__ scr, const NLConst& c,
                                                void* scan_mem, int tid, double* tau_out, double* fe_out,
@@ -258,7 +258,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
     const int p = tid % P;
     const int ch = tid / P;
     const int t0 = ch * 32;
-    float2* w = s + V::at(t0, p);   // this thread's 32 samples: w[walk_off<P>(i)]
+    float2* w = s + V::at(t0, p);   // this thread's 32 samples: w[V::walk(i)]
     const float2* dA = scr + t0 * P + p;   // dA of the same samples: dA[i * P]
     if (c.plasma) {
         MapR* mr = reinterpret_cast<MapR*>(scan_mem);
@@ -269,7 +269,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float B = 0.0f, C = 0.0f;
 #pragma unroll 8
             for (int i = 0; i < 32; i++) {
-                const IonPoint ip = ion_point(w[walk_off<P>(i)], c);
+                const IonPoint ip = ion_point(w[V::walk(i)], c);
                 const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
                 C = fmaf(1.0f - ip.b, C, Ck);
                 B = fmaf(-B, ip.b, B + ip.b);
@@ -313,7 +313,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
 #pragma unroll 4
         for (int i = 0; i < 32; i++) {
             const int t = t0 + i;
-            const float2 a = w[walk_off<P>(i)];
+            const float2 a = w[V::walk(i)];
             const IonPoint ip = ion_point(a, c);
             R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
             const float g = one_minus_exp_neg(R);
@@ -338,12 +338,12 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             const float amp = exp_small(c.dz * re);
             float sn, cs;
             sincos_small(c.dz * im, &sn, &cs);
-            w[walk_off<P>(i)] = cmul(a, make_float2(amp * cs, amp * sn));
+            w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
         }
     } else {
 #pragma unroll 4
         for (int i = 0; i < 32; i++) {
-            const float2 a = w[walk_off<P>(i)];
+            const float2 a = w[V::walk(i)];
             float re = 0.0f;
             float im = c.gam * fmaf(a.x, a.x, a.y * a.y);
             if (c.sst_c != 0.0f) {
@@ -354,7 +354,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             const float amp = exp_small(c.dz * re);
             float sn, cs;
             sincos_small(c.dz * im, &sn, &cs);
-            w[walk_off<P>(i)] = cmul(a, make_float2(amp * cs, amp * sn));
+            w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
         }
     }
 }
@@ -362,16 +362,21 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
 // ---------------------------------------------------------------------------------------
 // Pencil pass
 // ---------------------------------------------------------------------------------------
+// Shared memory of a pencil CTA: [field tile][scan maps][W_Nt twiddles][FP64 t sums (TEMP)].
+// One thread per 32-sample chunk: TH = P * Nt / 32 threads.
 template <int NT, int P, int SLO>
 struct PencilCfg {
     using View = PencilView<NT, P>;
     static constexpr int TPP = NT / 32;                 // 32-point chunks per pencil
+    static constexpr int TH = P * TPP;                  // threads per CTA
     static constexpr int SMEM_FIELD = View::SIZE * 8;  // bytes
     static constexpr int SMEM_SCAN = P * TPP * (int)sizeof(MapUV);
-    static constexpr int SMEM_TEMP = NT * 8;            // FP64 temporal sums (TEMP mode)
-    static constexpr int SMEM_TW = NT * 16;             // W_Nt twiddles
-    static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TEMP + SMEM_TW;
-    static_assert(NT * P == kTilePoints, "tile must hold 16384 points");
+    static constexpr int SMEM_TW = twiddle_bytes(NT);
+    static constexpr int SMEM_TEMP = NT * 8;            // FP64 temporal sums (TEMP mode only)
+    static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TW;
+    static constexpr int SMEM_TEMP_MODE = SMEM + SMEM_TEMP;
+    static constexpr int smem(int mode) { return mode == 5 ? SMEM_TEMP_MODE : SMEM; }
+    static_assert(TH % 32 == 0 && TH <= 1024, "pencil CTA size");
     static_assert((P * SLO) % 2 == 0, "rows must be whole float4s");
 };
 
@@ -381,7 +386,7 @@ template <int NT, int P, int SLO>
 __device__ __forceinline__ void prefetch_tile(const float2* g, int q0, int NP, int tid) {
     constexpr int ROWS = NT / SLO;
     constexpr int BYTES = P * SLO * 8;
-    for (int row = tid; row < ROWS; row += kThreads) {
+    for (int row = tid; row < ROWS; row += PencilCfg<NT, P, SLO>::TH) {
         const float2* a = g + ((size_t)row * NP + q0) * SLO;
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "n"(BYTES) : "memory");
     }
@@ -398,7 +403,7 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
     constexpr int F4_PER_ROW = P * SLO / 2;
     constexpr int ROWS = NT / SLO;
     const float4* g4 = reinterpret_cast<const float4*>(g);
-    for (int f = tid; f < ROWS * F4_PER_ROW; f += kThreads) {
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += PencilCfg<NT, P, SLO>::TH) {
         const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
         const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
         const float4 v = __ldg(&g4[gi]);
@@ -427,7 +432,7 @@ __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__
     constexpr int F4_PER_ROW = P * SLO / 2;
     constexpr int ROWS = NT / SLO;
     float4* g4 = reinterpret_cast<float4*>(g);
-    for (int f = tid; f < ROWS * F4_PER_ROW; f += kThreads) {
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += PencilCfg<NT, P, SLO>::TH) {
         const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
         const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
         int pos0, p0, pos1, p1;
@@ -446,22 +451,28 @@ __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__
 }
 
 template <int NT, int P, int SLO, int MODE>
-__global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
+__global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, SLO>::TH >= kThreads ? 1 : 2))
+    pencil_kernel(PencilArgs args) {
     using Cfg = PencilCfg<NT, P, SLO>;
     using V = typename Cfg::View;
-    constexpr int TPP = Cfg::TPP;
+    constexpr int TH = Cfg::TH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
     void* scan_mem = smem_raw + Cfg::SMEM_FIELD;
-    double* tsum = reinterpret_cast<double*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN);
+    unsigned char* tw_mem = smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN;
+    double* tsum = reinterpret_cast<double*>(smem_raw + Cfg::SMEM);
     const int tid = threadIdx.x;
     const int NP = args.NP;
-    float4* tw = reinterpret_cast<float4*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN + Cfg::SMEM_TEMP);
-    for (int k = tid; k < NT; k += kThreads) tw[k] = __ldg(&args.tw[k]);
+    {
+        const float* src = reinterpret_cast<const float*>(args.tw);
+        float* dst = reinterpret_cast<float*>(tw_mem);
+        for (int k = tid; k < 3 * NT; k += TH) dst[k] = __ldg(&src[k]);
+    }
+    const Twiddles tw = Twiddles::packed(tw_mem, NT);
     __syncthreads();
 
     if constexpr (MODE == PM_TEMP) {
-        for (int t = tid; t < NT; t += kThreads) tsum[t] = 0.0;
+        for (int t = tid; t < NT; t += TH) tsum[t] = 0.0;
         __syncthreads();
     }
 
@@ -473,7 +484,7 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
                 prefetch_tile<NT, P, SLO>(reinterpret_cast<const float2*>(args.in), nxt * P, NP, tid);
         }
         if constexpr (MODE == PM_IONIZ) {
-            for (int f = tid; f < NT * P; f += kThreads) {
+            for (int f = tid; f < NT * P; f += TH) {
                 const int t = f / P, p = f - (f / P) * P;
                 const size_t gi = (size_t)t * NP + q0 + p;
                 const double2 v = __ldg(&reinterpret_cast<const double2*>(args.in)[gi]);
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
             __syncthreads();
         } else if constexpr (MODE == PM_ENTRY_C128 || MODE == PM_ENTRY_C64) {
             // real-space input, reference layout A[t*NP + q]
-            for (int f = tid; f < NT * P; f += kThreads) {
+            for (int f = tid; f < NT * P; f += TH) {
                 const int t = f / P, p = f - (f / P) * P;
                 const size_t gi = (size_t)t * NP + q0 + p;
                 float2 e;
@@ -497,16 +508,16 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
                 s[V::at(t, p)] = e;
             }
             __syncthreads();
-            dif_all<NT, NT, V>(s, tw, tid, kThreads);
+            dif_all<NT, NT, V>(s, tw, tid, TH);
             store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         } else if constexpr (MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP) {
             load_tile<NT, P, SLO, false>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
             __syncthreads();
-            dit_all<NT, NT, V>(s, tw, tid, kThreads);
+            dit_all<NT, NT, V>(s, tw, tid, TH);
             if constexpr (MODE == PM_TEMP) {
                 const double inv = args.out_scale * args.out_scale;
-                for (int t = tid; t < NT; t += kThreads) {
+                for (int t = tid; t < NT; t += TH) {
                     float acc = 0.0f;
 #pragma unroll 8
                     for (int p = 0; p < P; p++) {
@@ -516,7 +527,7 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
                     tsum[t] += (double)acc * inv;
                 }
             } else {
-                for (int f = tid; f < NT * P; f += kThreads) {
+                for (int f = tid; f < NT * P; f += TH) {
                     const int t = f / P, p = f - (f / P) * P;
                     const size_t gi = (size_t)t * NP + q0 + p;
                     const float2 e = s[V::at(t, p)];
@@ -529,8 +540,8 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
                 }
                 // per-pencil energy sum_t |A|^2 (physical units)
                 if (args.pencil_energy) {
-                    const int p = tid % P, part = tid / P;           // kThreads/P partial sums per pencil
-                    constexpr int PARTS = kThreads / P;
+                    const int p = tid % P, part = tid / P;           // TH/P partial sums per pencil
+                    constexpr int PARTS = TH / P;
                     float acc = 0.0f;
                     for (int t = part; t < NT; t += PARTS) {
                         const float2 e = s[V::at(t, p)];
@@ -557,8 +568,8 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
             if (c.sst_c != 0.0f) {
                 load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
                 __syncthreads();
-                dit_all<NT, NT, V>(s, tw, tid, kThreads);
-                for (int f = tid; f < NT * P; f += kThreads) {
+                dit_all<NT, NT, V>(s, tw, tid, TH);
+                for (int f = tid; f < NT * P; f += TH) {
                     const int t = f / P, p = f - (f / P) * P;
                     scr[f] = s[V::at(t, p)];
                 }
@@ -567,18 +578,18 @@ __global__ void __launch_bounds__(kThreads, 1) pencil_kernel(PencilArgs args) {
             // A = IFFT_t(S)
             load_tile<NT, P, SLO, false>(s, gin, args.wpos, q0, NP, tid);
             __syncthreads();
-            dit_all<NT, NT, V>(s, tw, tid, kThreads);
+            dit_all<NT, NT, V>(s, tw, tid, TH);
 
             nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP);
             __syncthreads();
-            dif_all<NT, NT, V>(s, tw, tid, kThreads);
+            dif_all<NT, NT, V>(s, tw, tid, TH);
             store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         }
     }
     if constexpr (MODE == PM_TEMP) {
         __syncthreads();
-        for (int t = tid; t < NT; t += kThreads) atomicAdd(&args.temp[t], tsum[t]);
+        for (int t = tid; t < NT; t += TH) atomicAdd(&args.temp[t], tsum[t]);
     }
 }
 
@@ -597,8 +608,8 @@ struct PlaneTables {
 struct PlaneArgs {
     const float2* in;
     float2* out;
-    const float4* twx;       // W_Nx table {c, s, -eps, 0}
-    const float4* twy;
+    const float2* twx;       // W_Nx table, packed (mpc_fft.cuh Twiddles)
+    const float2* twy;       // W_Ny table, packed
     PlaneTables t1;      // first (or only) linear operator
     PlaneTables t2;      // second half after the mirror lens (lens != 0)
     const float2* lensx; // exp(-i k0 x^2 / roc), real x order
@@ -616,7 +627,7 @@ struct PlaneCfg {
     static constexpr int RS = CX + 1;    // padded row stride
     static constexpr int RSZ = PB * RY * RS;  // region (one partner block), complex64
     static constexpr int SIZE = CL * RSZ;
-    static constexpr int SMEM = SIZE * 8 + (NX + NY) * 16;
+    static constexpr int SMEM = SIZE * 8 + twiddle_bytes(NX) + twiddle_bytes(NY);
     static_assert(SLO == 1 || PB == SLO, "interleaved slots are processed together");
     static_assert((RSZ % 2) == 0, "regions are moved as float4");
 };
@@ -640,18 +651,18 @@ struct ColView {
 };
 
 // Swap region g of this CTA with region `rank` of CTA g, for every g != rank.
-template <int CL, int RSZ>
+template <int CL, int RSZ, int NTHR>
 __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& cluster, int rank, int tid) {
     if constexpr (CL > 1) {
         constexpr int F4 = RSZ / 2;               // float4 per region
         constexpr int KR = (CL >= 4) ? 2 : 1;     // partners per round
-        constexpr int PER = (KR * F4 + kThreads - 1) / kThreads;
+        constexpr int PER = (KR * F4 + NTHR - 1) / NTHR;
         cluster.sync();
         for (int k0 = 1; k0 < CL; k0 += KR) {
             float4 buf[PER];
 #pragma unroll
             for (int i = 0; i < PER; i++) {
-                const int f = tid + i * kThreads;
+                const int f = tid + i * NTHR;
                 if (f < KR * F4) {
                     const int kk = k0 + f / F4;
                     if (kk < CL) {
@@ -664,7 +675,7 @@ __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& c
             cluster.sync();
 #pragma unroll
             for (int i = 0; i < PER; i++) {
-                const int f = tid + i * kThreads;
+                const int f = tid + i * NTHR;
                 if (f < KR * F4) {
                     const int kk = k0 + f / F4;
                     if (kk < CL) {
@@ -678,18 +689,17 @@ __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& c
     }
 }
 
-template <int NX, int NY, int CL, int PB, int SLO>
+template <int NX, int NY, int CL, int PB, int SLO, int NTHR>
 __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, const PlaneTables& T, int rank, int unit,
-                                             const float4* twx, const float4* twy, cg::cluster_group& cluster,
-                                             int tid) {
+                                             Twiddles twx, Twiddles twy, cg::cluster_group& cluster, int tid) {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
     using CV = ColView<NX, NY, CL, PB, SLO>;
-    dif_all<NX, NX, RV>(s, twx, tid, kThreads);
-    cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
-    dif_all<NY, NY, CV>(s, twy, tid, kThreads);
+    dif_all<NX, NX, RV>(s, twx, tid, NTHR);
+    cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
+    dif_all<NY, NY, CV>(s, twy, tid, NTHR);
     // multiply by Rx(px) and Ry(py) D(slot) (double-float factors)
-    for (int e = tid; e < PB * NY * C::CX; e += kThreads) {
+    for (int e = tid; e < PB * NY * C::CX; e += NTHR) {
         const int xl = e % C::CX;
         const int r = e / C::CX;
         const int y = r % NY, pl = r / NY;
@@ -699,32 +709,37 @@ __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, cons
         s[idx] = cmul_df(cmul_df(s[idx], __ldg(&T.Rx[px])), __ldg(&T.RyD[(size_t)y * a.Nt + slot]));
     }
     __syncthreads();
-    dit_all<NY, NY, CV>(s, twy, tid, kThreads);
-    cluster_exchange<CL, C::RSZ>(s, cluster, rank, tid);
-    dit_all<NX, NX, RV>(s, twx, tid, kThreads);
+    dit_all<NY, NY, CV>(s, twy, tid, NTHR);
+    cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
+    dit_all<NX, NX, RV>(s, twx, tid, NTHR);
 }
 
-template <int NX, int NY, int CL, int PB, int SLO>
-__global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
+// NTHR threads per CTA; 512 / NTHR CTAs per SM (the register file holds 512 threads at
+// 128 registers).
+template <int NX, int NY, int CL, int PB, int SLO, int NTHR>
+__global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_kernel(PlaneArgs a) {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
-    float4* twx = reinterpret_cast<float4*>(smem_raw + C::SIZE * 8);
-    float4* twy = twx + NX;
+    unsigned char* twx_mem = smem_raw + C::SIZE * 8;
+    unsigned char* twy_mem = twx_mem + twiddle_bytes(NX);
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int tid = threadIdx.x;
     const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;
     const int NP = a.NP;
-    for (int k = tid; k < NX; k += kThreads) twx[k] = __ldg(&a.twx[k]);
-    for (int k = tid; k < NY; k += kThreads) twy[k] = __ldg(&a.twy[k]);
+    for (int k = tid; k < 3 * NX; k += NTHR)
+        reinterpret_cast<float*>(twx_mem)[k] = __ldg(&reinterpret_cast<const float*>(a.twx)[k]);
+    for (int k = tid; k < 3 * NY; k += NTHR)
+        reinterpret_cast<float*>(twy_mem)[k] = __ldg(&reinterpret_cast<const float*>(a.twy)[k]);
+    const Twiddles twx = Twiddles::packed(twx_mem, NX), twy = Twiddles::packed(twy_mem, NY);
     __syncthreads();
 
     for (int unit = cid; unit < a.nunits; unit += ncl) {
         // load this CTA's rows: y in [rank*RY, rank*RY + RY) of PB planes
         constexpr int F4_ROW = NX * SLO / 2;
-        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += kThreads) {
+        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += NTHR) {
             const int c = f % F4_ROW;
             const int r = f / F4_ROW;
             const int yl = r % C::RY, plb = r / C::RY;  // plb: plane block (SLO == 1: plane)
@@ -744,10 +759,10 @@ __global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
             }
         }
         __syncthreads();
-        plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t1, rank, unit, twx, twy, cluster, tid);
+        plane_linear<NX, NY, CL, PB, SLO, NTHR>(s, a, a.t1, rank, unit, twx, twy, cluster, tid);
         if (a.lens) {
             // mirror lens in real (x, y): exp(-i k0 (x^2 + y^2)/roc) = lensx[x] * lensy[y]
-            for (int e = tid; e < PB * C::RY * NX; e += kThreads) {
+            for (int e = tid; e < PB * C::RY * NX; e += NTHR) {
                 const int x = e % NX;
                 const int l = e / NX;
                 const int yl = l % C::RY;
@@ -756,9 +771,9 @@ __global__ void __launch_bounds__(kThreads, 1) plane_kernel(PlaneArgs a) {
                 s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y])));
             }
             __syncthreads();
-            plane_linear<NX, NY, CL, PB, SLO>(s, a, a.t2, rank, unit, twx, twy, cluster, tid);
+            plane_linear<NX, NY, CL, PB, SLO, NTHR>(s, a, a.t2, rank, unit, twx, twy, cluster, tid);
         }
-        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += kThreads) {
+        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += NTHR) {
             const int c = f % F4_ROW;
             const int r = f / F4_ROW;
             const int yl = r % C::RY, plb = r / C::RY;

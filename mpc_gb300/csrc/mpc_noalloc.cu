@@ -32,8 +32,8 @@ using mpc::NLConst;
 constexpr int kMaxCtas = 64;      // resident CTAs the dA area serves (grid is capped to it)
 constexpr int kMaxNt = 2048;      // longest t axis supported
 constexpr size_t kDABytes = (size_t)kMaxCtas * kTilePoints * sizeof(float2);   // 8 MiB
-constexpr size_t kTwOff = kDABytes;
-constexpr size_t kWposOff = kTwOff + (size_t)kMaxNt * sizeof(float4);
+constexpr size_t kTwOff = kDABytes;   // packed twiddle table (12 B per entry) in a 16 B-per-entry region
+constexpr size_t kWposOff = kTwOff + (size_t)kMaxNt * 16;
 constexpr size_t kWOff = kWposOff + (size_t)kMaxNt * sizeof(float);
 constexpr size_t kNoallocBytes = kWOff + (size_t)kMaxNt * sizeof(double);      // 8,445,952 B
 constexpr int kMaxDevices = 64;
@@ -113,16 +113,17 @@ bool nl_constants(const mpc_params& p, double fs, double dz, NLConst* out) {
     return true;
 }
 
-// Twiddles {c, s, -(c^2 + s^2 - 1), 0} of W_Nt^k and omega at each FFT position of the
-// in-place forward sweep (radices 16, ..., 16, r_last; pos = sum span_s k_s,
-// freq = k_1 + r_1 k_2 + ...), from the centred omega grid w.
-__global__ void k_noalloc_tables(int Nt, const double* w, float4* tw, float* wpos) {
+// Packed W_Nt table (mpc_fft.cuh Twiddles: (c, s) then -(c^2 + s^2 - 1)) and omega at each
+// FFT position of the in-place forward sweep (radices 16, ..., 16, r_last;
+// pos = sum span_s k_s, freq = k_1 + r_1 k_2 + ...), from the centred omega grid w.
+__global__ void k_noalloc_tables(int Nt, const double* w, float2* tw, float* wpos) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= Nt) return;
     double s, c;
     sincos(-2.0 * M_PI * (double)k / (double)Nt, &s, &c);
     const float cf = (float)c, sf = (float)s;
-    tw[k] = make_float4(cf, sf, (float)-((double)cf * cf + (double)sf * sf - 1.0), 0.0f);
+    tw[k] = make_float2(cf, sf);
+    reinterpret_cast<float*>(tw + Nt)[k] = (float)-((double)cf * cf + (double)sf * sf - 1.0);
     int rem = k, freq = 0, mult = 1;
     for (int L = Nt; L > 1;) {
         const int R = (L >= 16) ? 16 : L;
@@ -142,15 +143,18 @@ __global__ void k_noalloc_tables(int Nt, const double* w, float4* tw, float* wpo
 template <int NT, int P>
 __global__ void __launch_bounds__(kThreads, 1)
     k_nonlinear_noalloc(float2* A, int NP, int ntiles, float in_scale, float out_scale, NLConst c, float2* dA_area,
-                        const float4* tw_g, const float* wpos) {
+                        const float2* tw_g, const float* wpos) {
     using Cfg = mpc::PencilCfg<NT, P, 1>;
     using V = typename Cfg::View;
+    static_assert(Cfg::TH == kThreads, "one thread per 32-sample chunk");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
     void* scan_mem = smem_raw + Cfg::SMEM_FIELD;
-    float4* tw = reinterpret_cast<float4*>(smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN + Cfg::SMEM_TEMP);
+    unsigned char* tw_mem = smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN;
     const int tid = threadIdx.x;
-    for (int k = tid; k < NT; k += kThreads) tw[k] = tw_g[k];
+    for (int k = tid; k < 3 * NT; k += kThreads)
+        reinterpret_cast<float*>(tw_mem)[k] = reinterpret_cast<const float*>(tw_g)[k];
+    const mpc::Twiddles tw = mpc::Twiddles::packed(tw_mem, NT);
     __syncthreads();
     float2* scr = dA_area + (size_t)blockIdx.x * NT * P;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 struct NtKernel {
     int nt;
-    void (*fn)(float2*, int, int, float, float, NLConst, float2*, const float4*, const float*);
+    void (*fn)(float2*, int, int, float, float, NLConst, float2*, const float2*, const float*);
     int smem;
 };
 const NtKernel kKernels[] = {
@@ -258,7 +262,7 @@ extern "C" int mpc_nonlinear_noalloc(const mpc_params* p, void* A_dev, double dz
     }
     unsigned char* base = static_cast<unsigned char*>(g_dev_addr[dev]);
     float2* dA_area = reinterpret_cast<float2*>(base);
-    float4* tw = reinterpret_cast<float4*>(base + kTwOff);
+    float2* tw = reinterpret_cast<float2*>(base + kTwOff);
     float* wpos = reinterpret_cast<float*>(base + kWposOff);
     double* w = reinterpret_cast<double*>(base + kWOff);
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -1,11 +1,14 @@
 // mpc_shapes.cuh -- per-grid-shape launch configuration of the two sweeps.
 //
-// Tile and cluster shapes follow from shared-memory capacity (one 128 KB working set per
-// CTA, one CTA per SM) and the >= 128 B row rule for strided HBM access:
-//   pencil tile  P = 16384 / Nt pencils, SLO = 2 slots interleaved when P = 8, else 1;
-//   plane unit   SLO == 2: the two interleaved omega-planes, split over CL = bytes/128 KB CTAs;
-//                SLO == 1: planes over 128 KB are split over CL CTAs, smaller planes are
-//                batched PB per CTA.
+// A shape variant fixes the device layout and both sweeps' launch shapes:
+//   pencil tile  P = TP / Nt pencils, P * Nt / 32 threads per CTA (TP = 16384: one 512-thread
+//                CTA per SM; TP = 8192: two 256-thread CTAs per SM);
+//   SLO          slots interleaved in the layout (default 2 when P = 8, so t-rows are 128 B);
+//   plane unit   PT threads per CTA and 512 / PT CTAs per SM, each CTA holding a
+//                PLB = 128 KB * PT / 512 share of the unit; SLO == 2: the two interleaved
+//                omega-planes split over CL CTAs; SLO == 1: planes larger than PLB split over
+//                CL CTAs, smaller planes batched PB per CTA.
+// Several variants of one grid may be compiled in; they differ only in speed.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -14,42 +17,47 @@
 namespace mpc {
 
 struct ShapeOps {
-    int Nx, Ny, Nt, P, SLO, CL, PB;
+    int Nx, Ny, Nt, P, SLO, CL, PB, PT;
     int pencil_smem, plane_smem;
     cudaError_t (*setup)();
     cudaError_t (*pencil)(int mode, const PencilArgs&, int grid, cudaStream_t);
     cudaError_t (*plane)(const PlaneArgs&, int nclusters, cudaStream_t);
     int (*max_clusters)();
+    int (*pencil_blocks_per_sm)();   // resident split-step pencil CTAs per SM
 };
 
-template <int NX, int NY, int NT>
+template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints>
 struct Shape {
-    static constexpr int P = kTilePoints / NT;
-    static constexpr int SLO = (P < 16) ? 16 / P : 1;
+    static constexpr int P = TP / NT;
+    static constexpr int SLO = SLO_ > 0 ? SLO_ : ((P < 16) ? 16 / P : 1);
     static constexpr long PLANE_B = (long)NX * NY * 8;
-    static constexpr int CL = (SLO == 2) ? (int)(PLANE_B * 2 / 131072) : (PLANE_B > 131072 ? (int)(PLANE_B / 131072) : 1);
-    static constexpr int PB = (SLO == 2) ? 2 : (PLANE_B > 131072 ? 1 : ((131072 / PLANE_B) < NT ? (int)(131072 / PLANE_B) : NT));
-    static_assert(P >= 8 && P <= NX * NY, "pencil tile must fit the grid");
+    static constexpr long PLB = 131072L * PT / kThreads;
+    static constexpr int CL = (SLO == 2) ? (int)(PLANE_B * 2 / PLB) : (PLANE_B > PLB ? (int)(PLANE_B / PLB) : 1);
+    static constexpr int PB = (SLO == 2) ? 2 : (PLANE_B > PLB ? 1 : ((PLB / PLANE_B) < NT ? (int)(PLB / PLANE_B) : NT));
+    static_assert(SLO == 1 || SLO == 2, "slot interleave");
+    static_assert(PT == 128 || PT == 256 || PT == 512, "plane threads");
+    static_assert(P >= 4 && P <= NX * NY, "pencil tile must fit the grid");
     static_assert(CL >= 1 && CL <= 16 && NY % CL == 0 && NX % CL == 0, "cluster split");
     using PC = PencilCfg<NT, P, SLO>;
     using LC = PlaneCfg<NX, NY, CL, PB, SLO>;
+    static constexpr int TH = PC::TH;
 
     static cudaError_t setup() {
         cudaError_t e;
 #define MPC_SET_SMEM(K, B)                                                                       \
     e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, B);                   \
     if (e != cudaSuccess) return e;
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C128>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C64>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_STEP>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C128>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP>), PC::SMEM);
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ>), PC::SMEM);
-        MPC_SET_SMEM((plane_kernel<NX, NY, CL, PB, SLO>), LC::SMEM);
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C128>), PC::smem(PM_ENTRY_C128));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C64>), PC::smem(PM_ENTRY_C64));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_STEP>), PC::smem(PM_STEP));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C128>), PC::smem(PM_EXIT_C128));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64>), PC::smem(PM_EXIT_C64));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP>), PC::smem(PM_TEMP));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ>), PC::smem(PM_IONIZ));
+        MPC_SET_SMEM((plane_kernel<NX, NY, CL, PB, SLO, PT>), LC::SMEM);
 #undef MPC_SET_SMEM
         if (CL > 8) {
-            e = cudaFuncSetAttribute(plane_kernel<NX, NY, CL, PB, SLO>,
+            e = cudaFuncSetAttribute(plane_kernel<NX, NY, CL, PB, SLO, PT>,
                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
             if (e != cudaSuccess) return e;
         }
@@ -58,13 +66,13 @@ struct Shape {
 
     static cudaError_t pencil(int mode, const PencilArgs& a, int grid, cudaStream_t st) {
         switch (mode) {
-            case PM_ENTRY_C128: pencil_kernel<NT, P, SLO, PM_ENTRY_C128><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_ENTRY_C64: pencil_kernel<NT, P, SLO, PM_ENTRY_C64><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_STEP: pencil_kernel<NT, P, SLO, PM_STEP><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_EXIT_C128: pencil_kernel<NT, P, SLO, PM_EXIT_C128><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_EXIT_C64: pencil_kernel<NT, P, SLO, PM_EXIT_C64><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_TEMP: pencil_kernel<NT, P, SLO, PM_TEMP><<<grid, kThreads, PC::SMEM, st>>>(a); break;
-            case PM_IONIZ: pencil_kernel<NT, P, SLO, PM_IONIZ><<<grid, kThreads, PC::SMEM, st>>>(a); break;
+            case PM_ENTRY_C128: pencil_kernel<NT, P, SLO, PM_ENTRY_C128><<<grid, TH, PC::smem(PM_ENTRY_C128), st>>>(a); break;
+            case PM_ENTRY_C64: pencil_kernel<NT, P, SLO, PM_ENTRY_C64><<<grid, TH, PC::smem(PM_ENTRY_C64), st>>>(a); break;
+            case PM_STEP: pencil_kernel<NT, P, SLO, PM_STEP><<<grid, TH, PC::smem(PM_STEP), st>>>(a); break;
+            case PM_EXIT_C128: pencil_kernel<NT, P, SLO, PM_EXIT_C128><<<grid, TH, PC::smem(PM_EXIT_C128), st>>>(a); break;
+            case PM_EXIT_C64: pencil_kernel<NT, P, SLO, PM_EXIT_C64><<<grid, TH, PC::smem(PM_EXIT_C64), st>>>(a); break;
+            case PM_TEMP: pencil_kernel<NT, P, SLO, PM_TEMP><<<grid, TH, PC::smem(PM_TEMP), st>>>(a); break;
+            case PM_IONIZ: pencil_kernel<NT, P, SLO, PM_IONIZ><<<grid, TH, PC::smem(PM_IONIZ), st>>>(a); break;
             default: return cudaErrorInvalidValue;
         }
         return cudaGetLastError();
@@ -73,7 +81,7 @@ struct Shape {
     static cudaError_t plane(const PlaneArgs& a, int nclusters, cudaStream_t st) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(nclusters * CL);
-        cfg.blockDim = dim3(kThreads);
+        cfg.blockDim = dim3(PT);
         cfg.dynamicSmemBytes = LC::SMEM;
         cfg.stream = st;
         cudaLaunchAttribute attr[1];
@@ -83,13 +91,13 @@ struct Shape {
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, plane_kernel<NX, NY, CL, PB, SLO>, a);
+        return cudaLaunchKernelEx(&cfg, plane_kernel<NX, NY, CL, PB, SLO, PT>, a);
     }
 
     static int max_clusters() {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(CL);
-        cfg.blockDim = dim3(kThreads);
+        cfg.blockDim = dim3(PT);
         cfg.dynamicSmemBytes = LC::SMEM;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -99,12 +107,21 @@ struct Shape {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, plane_kernel<NX, NY, CL, PB, SLO>, &cfg) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveClusters(&n, plane_kernel<NX, NY, CL, PB, SLO, PT>, &cfg) != cudaSuccess) return 0;
+        return n;
+    }
+
+    static int pencil_blocks_per_sm() {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pencil_kernel<NT, P, SLO, PM_STEP>, TH, PC::SMEM) !=
+            cudaSuccess)
+            return 0;
         return n;
     }
 
     static const ShapeOps* ops() {
-        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PC::SMEM, LC::SMEM, &setup, &pencil, &plane, &max_clusters};
+        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PT, PC::SMEM, LC::SMEM, &setup, &pencil, &plane,
+                                   &max_clusters, &pencil_blocks_per_sm};
         return &o;
     }
 };

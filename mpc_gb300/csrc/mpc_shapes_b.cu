@@ -1,10 +1,12 @@
-// Kernel instantiations for grid shapes: 128,128,1024 256,256,512 (Nx,Ny,Nt).
+// Kernel instantiations for grid shapes: 128,128,1024 256,256,512 (Nx,Ny,Nt), two variants each.
 #include "mpc_shapes.cuh"
 
 namespace mpc {
 extern const ShapeOps* const shape_list_b[];
 const ShapeOps* const shape_list_b[] = {
     Shape<128,128,1024>::ops(),
+    Shape<128,128,1024,1,256>::ops(),   // plane 256 threads x 2 per SM, clusters of 2
     Shape<256,256,512>::ops(),
+    Shape<256,256,512,1,256>::ops(),    // plane 256 threads x 2 per SM, clusters of 8
     nullptr};
 }  // namespace mpc

@@ -1,9 +1,13 @@
-// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt).
+// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt), four layout / launch
+// variants (all give identical results; variant 0 is the default, the autotuner times all).
 #include "mpc_shapes.cuh"
 
 namespace mpc {
 extern const ShapeOps* const shape_list_c[];
 const ShapeOps* const shape_list_c[] = {
-    Shape<256,256,2048>::ops(),
+    Shape<256,256,2048,1,256>::ops(),      // SLO 1, plane 256 threads x 2 per SM, clusters of 8
+    Shape<256,256,2048>::ops(),            // SLO 2, plane 512 threads, clusters of 8 (2 planes)
+    Shape<256,256,2048,1,512>::ops(),      // SLO 1, plane 512 threads, clusters of 4
+    Shape<256,256,2048,1,256,8192>::ops(), // SLO 1, 4-pencil tiles, 256-thread pencil and plane CTAs
     nullptr};
 }  // namespace mpc

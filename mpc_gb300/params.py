@@ -6,7 +6,8 @@ double wr[Ny]; int sst_on; double w[Nt]; double gamma2, w0; int plasm; double de
 rho_c, rho_nt, n0, puls_e, Ab_M; double r[Ny]; double dr, def_err, dzmin, Esig;
 char gas[9].  Fields and units are those of the reference; bounce_mode and roc describe
 the mirror, which the reference models only as a diffraction sign flip and which
-param.bin therefore does not carry.
+param.bin therefore does not carry; variant picks among the compiled kernel variants of a
+grid (speed only).
 """
 from __future__ import annotations
 
@@ -48,6 +49,7 @@ class MPCParams:
     gas: str
     bounce_mode: int = BOUNCE_SIGNFLIP
     roc: float = 0.0
+    variant: int = 0          # compiled kernel variant of the grid (0 default, -1 autotune)
 
     @property
     def Nx(self) -> int:

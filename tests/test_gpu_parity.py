@@ -178,3 +178,34 @@ def test_create_destroy_leaves_no_pending_error(gpu_lib):
     with Propagator(p) as prop:
         prop.ssfmprop(A.copy(), p.dzz, 1, 0.0, p.puls_e, change=1)
     assert cudart.cudaGetLastError() == 0
+
+
+@pytest.mark.parametrize("grid", [(64, 64, 512), (128, 128, 1024), (256, 256, 512), (256, 256, 2048)])
+def test_kernel_variants_agree(gpu_lib, grid):
+    """Every compiled kernel variant of a grid (device layout, tile and launch shapes) gives the
+    same field after 6 split steps; an index past the last variant is rejected; the
+    autotuner (variant = -1) picks one of them."""
+    from mpc_gb300.capi import MPCError, Propagator
+    Nx, Ny, Nt = grid
+    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048)
+    p0, A = inputs.make_cell(cfg)
+    ref = None
+    v = 0
+    while True:
+        try:
+            prop = Propagator(p0.copy(variant=v))
+        except MPCError:
+            break
+        with prop:
+            assert prop.variant_info()["variant"] == v
+            prop.upload(A, calibrate=True)
+            prop.run_fixed(6)
+            out = prop.download()
+        if ref is None:
+            ref = out
+        else:
+            assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-6, v
+        v += 1
+    assert v >= 2
+    with Propagator(p0.copy(variant=-1)) as prop:
+        assert 0 <= prop.variant_info()["variant"] < v

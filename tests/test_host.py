@@ -123,31 +123,46 @@ def test_position_frequency_table(N):
     assert sorted(closed) == list(range(N))
 
 
-SHAPES = [(16, 16, 64), (32, 32, 256), (64, 64, 512), (128, 128, 1024), (256, 256, 512), (256, 256, 2048),
-          (512, 512, 1024)]
+def _compiled_variants():
+    """(Nx, Ny, Nt, SLO, PT, TP) of every Shape<...>::ops() entry of the shape lists."""
+    import glob
+    import re
+    out = []
+    for f in sorted(glob.glob(os.path.join(ROOT, "mpc_gb300", "csrc", "mpc_shapes_*.cu"))):
+        for m in re.finditer(r"Shape<([\d,\s]+)>::ops\(\)", open(f).read()):
+            v = [int(x) for x in m.group(1).split(",")]
+            v += [0, 512, 16384][len(v) - 3:]
+            out.append(tuple(v))
+    return out
 
 
-def _shape_cfg(NX, NY, NT):
+SHAPES = _compiled_variants()
+
+
+def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384):
     """Tile and cluster parameters, as mpc_shapes.cuh derives them."""
-    P = 16384 // NT
-    SLO = 16 // P if P < 16 else 1
+    P = TP // NT
+    SLO = SLO_ if SLO_ > 0 else (16 // P if P < 16 else 1)
     plane_b = NX * NY * 8
+    plb = 131072 * PT // 512
     if SLO == 2:
-        CL, PB = plane_b * 2 // 131072, 2
-    elif plane_b > 131072:
-        CL, PB = plane_b // 131072, 1
+        CL, PB = plane_b * 2 // plb, 2
+    elif plane_b > plb:
+        CL, PB = plane_b // plb, 1
     else:
-        CL, PB = 1, min(131072 // plane_b, NT)
+        CL, PB = 1, min(plb // plane_b, NT)
     return P, SLO, CL, PB
 
 
-def _views(NX, NY, NT):
+def _views(*variant):
     """Python statement of the shared-memory views of mpc_kernels.cuh:
     (name, N, NLINES, at(pos, line), size)."""
-    P, SLO, CL, PB = _shape_cfg(NX, NY, NT)
+    NX, NY, NT = variant[:3]
+    P, SLO, CL, PB = _shape_cfg(*variant)
     if P < 16:
-        pen = lambda pos, l: pos * P + l + P * ((pos >> 4) + (pos >> 5))  # noqa: E731
-        psize = NT * P + P * (NT // 16 + NT // 32)
+        SH = 3 if P < 8 else 4
+        pen = lambda pos, l: pos * P + l + P * ((pos >> SH) + (pos >> 5))  # noqa: E731
+        psize = NT * P + P * ((NT >> SH) + NT // 32)
     else:
         pen = lambda pos, l: pos * P + l  # noqa: E731
         psize = NT * P
@@ -163,12 +178,52 @@ def _views(NX, NY, NT):
     return [("pencil", NT, P, pen, psize), ("row", NX, PB * RY, row, CL * RSZ), ("col", NY, PB * CX, col, CL * RSZ)]
 
 
+def test_variant_list_parsed():
+    assert (256, 256, 2048, 0, 512, 16384) in SHAPES
+    assert len({v[:3] for v in SHAPES}) >= 7
+
+
+def _wavefronts(addrs):
+    """Shared-memory wavefronts of one warp-wide 8-byte access (32 four-byte banks)."""
+    rows = {}
+    for a in addrs:
+        for w in (2 * a, 2 * a + 1):
+            rows.setdefault(w % 32, set()).add(w // 32)
+    return max(len(r) for r in rows.values())
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_pencil_view_bank_conflict_free(shape):
+    """Every FFT stage of the pencil tile and the 32-sample t walk of the nonlinear step take
+    the minimum two wavefronts per warp access (no bank conflicts)."""
+    name, N, P, at, size = _views(*shape)[0]
+    nthr = N * P // 32
+    L = N
+    while L > 1:
+        R = 16 if L >= 16 else L
+        S = L // R
+        for w0 in range(0, min(N // R * P, nthr), 32):
+            for q in range(R):
+                addrs = []
+                for idx in range(w0, w0 + 32):
+                    line, g = idx % P, idx // P
+                    addrs.append(at((g // S) * L + g % S + S * q, line))
+                assert _wavefronts(addrs) <= 2, (shape, L, w0, q)
+        L //= R
+    for i in range(32):
+        assert _wavefronts([at(32 * (t // P) + i, t % P) for t in range(32)]) <= 2, (shape, i)
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 def test_fft_views_stage_separable_and_in_bounds(shape):
     """The FFT stages address a butterfly as at(base) + at(S q) - at(0) (mpc_fft.cuh); check
     that this equals at(base + S q) for every view, stage and butterfly, that every address
     is inside the view's shared-memory buffer, and that the view is one-to-one."""
     for name, N, NL, at, size in _views(*shape):
+        if name == "pencil":   # the walk offsets of the nonlinear step equal at(t0 + i) - at(t0)
+            for t0 in range(0, N, 32):
+                for i in range(32):
+                    assert at(t0 + i, 0) - at(t0, 0) == at(i, 0) - at(0, 0), (t0, i)
         seen = set()
         for pos in range(N):
             for l in range(NL):
