@@ -125,6 +125,24 @@ int mpc_set_state(mpc_ctx *ctx, const mpc_state *st);
  * flip) at every multiple of Cav.  Updates state.z, nstep, puls_e. */
 int mpc_run_fixed(mpc_ctx *ctx, int nsteps);
 
+/* One attempt of the reference's adaptive step (the body of the MPC.c:269-383 loop, with
+ * the defects corrected) on the device-resident field: C1 = one split step of 2*dzz and
+ * C2 = two split steps of dzz from the same field, the diffraction sign taken from state.z
+ * for all three (calcexpR, propagation.c:375-391); err = |C2 - C1| / |C2| reduced on the
+ * device in FP64, and setStep's rule (propagation.c:616-677) picks the next state.dzz.
+ * Accepted (*bad = 0): the field becomes (4 C2 - C1) / 3, state.z advances by 2*dzz (the step
+ * just taken), each mirror plane crossed applies a bounce (the lens phase in lens mode, the
+ * mirror loss Ab_M on puls_e), nstep += 1.  Rejected (*bad = 1): the field is unchanged and
+ * state.dzz halved.  BP1 (Nx) and BP2 (Ny) receive C2's beam profiles (NULL to skip); state
+ * y1, y2, bps1, bps2 are updated from them; attempts += 1. */
+int mpc_step_double(mpc_ctx *ctx, double *BP1, double *BP2, int *bad, double *err);
+
+/* One mirror bounce of the device-resident field, now: MPC_BOUNCE_LENS multiplies it by the
+ * mirror's focusing phase exp(-i k0 (x^2 + y^2) / roc); MPC_BOUNCE_SIGNFLIP flips
+ * state.signmem, the reference's bookkeeping of a bounce (propagation.c:334-341; the
+ * diffraction sign of later steps follows from z).  Either way state.puls_e *= Ab_M. */
+int mpc_mirror_bounce(mpc_ctx *ctx, int mode);
+
 /* Diagnostics of the device-resident field (MPC.c:389-449, propagation.c:343-361):
  * temp[Nt] = sum_xy |A|^2, spec[Nt] = sum_xy |FFT_t A|^2 (FFT order), BP1[Nx], BP2[Ny];
  * any pointer may be NULL. */

@@ -61,6 +61,8 @@ SIGNATURES = {
     "mpc_get_state": (C.c_int, [C.c_void_p, C.POINTER(c_mpc_state)]),
     "mpc_set_state": (C.c_int, [C.c_void_p, C.POINTER(c_mpc_state)]),
     "mpc_run_fixed": (C.c_int, [C.c_void_p, C.c_int]),
+    "mpc_step_double": (C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp]),
+    "mpc_mirror_bounce": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_diag": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
     "mpc_energy": (C.c_int, [C.c_void_p, _dp]),
     "mpc_sync": (C.c_int, [C.c_void_p]),
@@ -229,6 +231,23 @@ class Propagator:
 
     def run_fixed(self, nsteps: int) -> None:
         _check(self.lib.mpc_run_fixed(self.h, nsteps), "mpc_run_fixed")
+
+    def step_double(self, profiles: bool = False):
+        """One adaptive step-doubling attempt on the device field (MPC.c:269-383).
+        Returns dict(bad, err[, BP1, BP2])."""
+        bad = C.c_int(0)
+        err = C.c_double(0)
+        BP1 = np.zeros(self.p.Nx) if profiles else None
+        BP2 = np.zeros(self.p.Ny) if profiles else None
+        _check(self.lib.mpc_step_double(self.h, _ptr(BP1) if profiles else None, _ptr(BP2) if profiles else None,
+                                        C.byref(bad), C.byref(err)), "mpc_step_double")
+        out = dict(bad=bad.value, err=err.value)
+        if profiles:
+            out.update(BP1=BP1, BP2=BP2)
+        return out
+
+    def mirror_bounce(self, mode: int) -> None:
+        _check(self.lib.mpc_mirror_bounce(self.h, int(mode)), "mpc_mirror_bounce")
 
     def diag(self):
         temp = np.zeros(self.p.Nt)

@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -165,6 +166,39 @@ __global__ void k_diffnorm_c128(const double2* __restrict__ a, const double2* __
     }
 }
 
+// Richardson combination and error sums of one step-doubling attempt (MPC.c:350-381 and
+// propagation.c:624-633, on the device field): out = (4 C2 - C1) / 3 (out may alias C1),
+// sums[0] += |C2 - C1|^2, sums[1] += |C2|^2, accumulated in FP64.
+__global__ void k_richardson(const float2* C1, const float2* C2, float2* out, long n, double* sums) {
+    __shared__ double sh[32];
+    double s1 = 0.0, s2 = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float2 a = C1[i], b = C2[i];
+        const float dx = b.x - a.x, dy = b.y - a.y;
+        s1 += (double)fmaf(dx, dx, dy * dy);
+        s2 += (double)fmaf(b.x, b.x, b.y * b.y);
+        out[i] = make_float2(fmaf(4.0f / 3.0f, b.x, -a.x / 3.0f), fmaf(4.0f / 3.0f, b.y, -a.y / 3.0f));
+    }
+    s1 = block_sum(s1, sh);
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) {
+        atomicAdd(sums, s1);
+        atomicAdd(sums + 1, s2);
+    }
+}
+
+// E[q] = scale * sum over the Nt slots of |S[slot, q]|^2 (slot layout), one thread per pencil
+__global__ void k_pencil_energy_slots(const float2* __restrict__ S, int NP, int Nt, int SLO, double scale, double* E) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= NP) return;
+    double acc = 0.0;
+    for (int s = 0; s < Nt; s++) {
+        const float2 v = S[((size_t)(s / SLO) * NP + q) * SLO + (s % SLO)];
+        acc += (double)fmaf(v.x, v.x, v.y * v.y);
+    }
+    E[q] = acc * scale;
+}
+
 // spec[freq(pos)] = scale * sum_q |S[pos, q]|^2 for the slot layout; one block per slot
 __global__ void k_spec(const float2* __restrict__ S, int NP, int SLO, const int* ft, double scale, double* spec) {
     __shared__ double sh[32];
@@ -235,6 +269,7 @@ struct mpc_ctx {
     double2* io = nullptr;      // complex128 staging, N
     double2* io2 = nullptr;     // second complex128 staging (setStep)
     float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;  // packed twiddle tables
+    float2 *C1 = nullptr, *C2 = nullptr;                    // step doubling (allocated on first use)
     float* wpos = nullptr;
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
     std::vector<int> hfx, hfy, hft;
@@ -511,7 +546,7 @@ int mpc_destroy(mpc_ctx* c) {
     // and lensx, and cudaFree of an interior pointer fails and leaves an error pending in the
     // (process-wide) runtime for the caller's next CUDA call
     void* ptrs[] = {c->S,   c->scratch, c->io,  c->io2,     c->twx,    c->twy,  c->twt,
-                    c->wpos, c->dfx,    c->dwr, c->lensx,   c->penergy, c->dred};
+                    c->wpos, c->dfx,    c->dwr, c->lensx,   c->penergy, c->dred, c->C1, c->C2};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->st) cudaStreamDestroy(c->st);
@@ -656,7 +691,7 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
 // context of its own, timed with CUDA events over the last 3.  The choice is cached per device
 // and grid for the life of the process.  The nonlinear step's cost depends on the field, but
 // the shapes compared here do not change that part.
-static int pencil_step(mpc_ctx* c, double dz);
+static int pencil_step(mpc_ctx* c, double dz, float2* buf);
 
 static int autotune_variant(const mpc_params* p, int* best) {
     static std::mutex mu;
@@ -690,7 +725,7 @@ static int autotune_variant(const mpc_params* p, int* best) {
         ok = ok && get_tables(c, q.dzz, q.dzz, 1.0 / ((double)c->NP * c->Nt), &t) == MPC_OK;
         for (int i = 0; ok && i < 5; i++) {
             if (i == 2) ok = cudaEventRecord(e0, c->st) == cudaSuccess;
-            ok = ok && pencil_step(c, q.dzz) == MPC_OK && launch_plane(c, c->S, c->S, t, nullptr) == MPC_OK;
+            ok = ok && pencil_step(c, q.dzz, nullptr) == MPC_OK && launch_plane(c, c->S, c->S, t, nullptr) == MPC_OK;
         }
         ok = ok && cudaEventRecord(e1, c->st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
              cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
@@ -818,11 +853,11 @@ int mpc_field_download(mpc_ctx* c, double* A) {
     return MPC_OK;
 }
 
-// one nonlinear step of the pencil sweep, in place on S
-static int pencil_step(mpc_ctx* c, double dz) {
+// one nonlinear step of the pencil sweep, in place on buf (default: the field S)
+static int pencil_step(mpc_ctx* c, double dz, float2* buf = nullptr) {
     PencilArgs a{};
-    a.in = c->S;
-    a.out = c->S;
+    a.in = buf ? buf : c->S;
+    a.out = buf ? buf : c->S;
     a.nl = c->nl;
     a.nl.dz = (float)dz;
     return launch_pencil(c, mpc::PM_STEP, a);
@@ -1145,6 +1180,99 @@ int mpc_diag(mpc_ctx* c, double* temp, double* spec, double* BP1, double* BP2) {
         if (BP2) CK(cudaMemcpyAsync(BP2, d2, sizeof(double) * c->Ny, cudaMemcpyDeviceToHost, c->st), "D2H BP2");
         CK(cudaStreamSynchronize(c->st), "beam profiles");
     }
+    return MPC_OK;
+}
+
+int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err) {
+    if (!c || !bad || !err) return fail(MPC_ERR_ARG, "null argument");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    for (float2** b : {&c->C1, &c->C2})
+        if (!*b && cudaMalloc(b, sizeof(float2) * c->N) != cudaSuccess) {
+            *b = nullptr;
+            cudaGetLastError();
+            return fail(MPC_ERR_NOMEM, "cudaMalloc step-doubling fields");
+        }
+    mpc_state& st = c->state;
+    const double dz = st.dzz, Cav = c->p.Cav;
+    // calcexpR's sign logic (propagation.c:377-382), evaluated at the attempt's z for all three steps
+    int signum = pass_sign(st.z, Cav);
+    if (-st.signmem == signum) st.signmem = -st.signmem;
+    if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
+    const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
+    int rc;
+    // C1: one step of 2 dz
+    TableSet a1, a2;
+    if ((rc = get_tables(c, signum * dz, dz, sNP, &a1))) return rc;
+    if ((rc = get_tables(c, signum * dz, dz, sN, &a2))) return rc;
+    if ((rc = launch_plane(c, c->S, c->C1, a1, nullptr))) return rc;
+    if ((rc = pencil_step(c, 2.0 * dz, c->C1))) return rc;
+    if ((rc = launch_plane(c, c->C1, c->C1, a2, nullptr))) return rc;
+    // C2: two steps of dz, the two middle half steps merged
+    TableSet b1, bm, b2;
+    if ((rc = get_tables(c, signum * dz / 2, dz / 2, sNP, &b1))) return rc;
+    if ((rc = get_tables(c, signum * dz, dz, sN, &bm))) return rc;
+    if ((rc = get_tables(c, signum * dz / 2, dz / 2, sN, &b2))) return rc;
+    if ((rc = launch_plane(c, c->S, c->C2, b1, nullptr))) return rc;
+    if ((rc = pencil_step(c, dz, c->C2))) return rc;
+    if ((rc = launch_plane(c, c->C2, c->C2, bm, nullptr))) return rc;
+    if ((rc = pencil_step(c, dz, c->C2))) return rc;
+    if ((rc = launch_plane(c, c->C2, c->C2, b2, nullptr))) return rc;
+    // beam profiles of C2 (the change == 1 step, propagation.c:343-361), physical units:
+    // sum_t |A|^2 = Nt sum_omega |S|^2 / fs^2
+    k_pencil_energy_slots<<<(int)((c->NP + 255) / 256), 256, 0, c->st>>>(c->C2, (int)c->NP, c->Nt, c->ops->SLO,
+                                                                       (double)c->Nt / (c->fs * c->fs), c->penergy);
+    CK(cudaGetLastError(), "k_pencil_energy_slots");
+    double* dbp = c->dred + 2;
+    k_beam_profiles<<<(c->Nx + 255) / 256, 256, 0, c->st>>>(c->penergy, c->Nx, c->Ny, dbp, dbp + c->Nx);
+    CK(cudaGetLastError(), "k_beam_profiles");
+    // error sums and the Richardson field (into C1)
+    CK(cudaMemsetAsync(c->dred, 0, 2 * sizeof(double), c->st), "memset");
+    k_richardson<<<c->nsm * 4, 256, 0, c->st>>>(c->C1, c->C2, c->C1, c->N, c->dred);
+    CK(cudaGetLastError(), "k_richardson");
+    std::vector<double> h(2 + c->Nx + c->Ny);
+    CK(cudaMemcpyAsync(h.data(), c->dred, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->st), "D2H sums");
+    CK(cudaStreamSynchronize(c->st), "step_double");
+    mpc_calc1oes(h.data() + 2, c->Nx, c->r.data(), &st.bps1, st.y1);
+    mpc_calc1oes(h.data() + 2 + c->Nx, c->Ny, c->r.data(), &st.bps2, st.y2);
+    if (BP1) memcpy(BP1, h.data() + 2, sizeof(double) * c->Nx);
+    if (BP2) memcpy(BP2, h.data() + 2 + c->Nx, sizeof(double) * c->Ny);
+    *err = sqrt(h[0]) / sqrt(h[1]);
+    st.err = *err;
+    step_rule(*err, &st.dzz, c->p.def_err, c->p.dzmin, st.y1, st.y2, bad);
+    st.bad = *bad;
+    st.attempts++;
+    if (*bad) return MPC_OK;
+    std::swap(c->S, c->C1);  // the accepted field (4 C2 - C1)/3
+    const double z0 = st.z;
+    st.z = z0 + 2.0 * dz;    // A26: the step just taken
+    const int nb = bounces_between(z0, st.z, Cav);
+    for (int b = 0; b < nb; b++) {
+        if (c->p.bounce_mode == MPC_BOUNCE_LENS && (rc = launch_plane(c, c->S, c->S, c->ident, &c->ident))) return rc;
+        st.puls_e *= c->p.Ab_M;  // A24: the mirror loss the reference's bookkeeping never applies
+    }
+    if (st.z > c->p.dist) st.z = c->p.dist;
+    st.nstep++;
+    return MPC_OK;
+}
+
+int mpc_mirror_bounce(mpc_ctx* c, int mode) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    if (mode == MPC_BOUNCE_LENS) {
+        if (c->p.roc == 0.0) return fail(MPC_ERR_ARG, "lens bounce needs the mirror radius of curvature roc");
+        if (c->p.bounce_mode != MPC_BOUNCE_LENS) {
+            k_lens<<<(c->Nx + 255) / 256, 256, 0, c->st>>>(c->dr, c->Nx, c->p.k0, c->p.roc, c->lensx);
+            k_lens<<<(c->Ny + 255) / 256, 256, 0, c->st>>>(c->dr, c->Ny, c->p.k0, c->p.roc, c->lensy);
+            CK(cudaGetLastError(), "k_lens");
+        }
+        int rc = launch_plane(c, c->S, c->S, c->ident, &c->ident);
+        if (rc) return rc;
+    } else if (mode == MPC_BOUNCE_SIGNFLIP) {
+        c->state.signmem = -c->state.signmem;
+    } else {
+        return fail(MPC_ERR_ARG, "unknown bounce mode");
+    }
+    c->state.puls_e *= c->p.Ab_M;
     return MPC_OK;
 }
 

@@ -209,3 +209,62 @@ def test_kernel_variants_agree(gpu_lib, grid):
     assert v >= 2
     with Propagator(p0.copy(variant=-1)) as prop:
         assert 0 <= prop.variant_info()["variant"] < v
+
+
+@pytest.mark.parametrize("bounce", [BOUNCE_LENS, BOUNCE_SIGNFLIP])
+def test_step_double_matches_oracle(gpu_lib, bounce):
+    """Adaptive step-doubling attempts (MPC.c:269-383) on the device field against the
+    oracle's, until the pulse has crossed a mirror plane: the same accept/reject decisions,
+    step sizes, z, mirror bounces and loss, beam sizes, and the field within the multi-step
+    tolerance."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(energy=2e-3, fwhm=150e-15, pressure=2.0, bounce=bounce, steps_per_pass=4, Ab_M=0.9,
+                         def_err=3e-4)
+    o2 = oracle.Oracle(p)
+    ref = A.copy()
+    C1 = np.empty_like(ref)
+    C2 = np.empty_like(ref)
+    st = o2.new_state()
+    decisions = []
+    with Propagator(p) as prop:
+        prop.upload(A)
+        for k in range(80):
+            if st.z > p.Cav + 2 * st.dzz:
+                break
+            o2.double_step(ref, C1, C2, st)
+            r = prop.step_double(profiles=True)
+            s = prop.state()
+            decisions.append(r["bad"])
+            assert r["bad"] == st.bad, k
+            assert abs(r["err"] / st.err - 1) < 0.05, (k, r["err"], st.err)
+            assert s.dzz == pytest.approx(st.dzz, rel=1e-12) and s.z == pytest.approx(st.z, rel=1e-12, abs=1e-15)
+            assert s.nstep == st.nstep and s.attempts == st.attempts and s.signmem == st.signmem
+            assert s.puls_e == pytest.approx(st.puls_e, rel=1e-12)
+            # beam sizes from C2's profiles: crossing positions on the r grid, profile values
+            assert list(s.y1)[:2] == list(st.y1)[:2] and list(s.y2)[:2] == list(st.y2)[:2], k
+            assert list(s.y1)[2:] == pytest.approx(list(st.y1)[2:], rel=1e-4)
+            assert s.bps1 == pytest.approx(st.bps1, rel=1e-12) and r["BP1"].max() > 0
+        got = prop.download()
+    assert 0 in decisions and 1 in decisions          # both branches exercised
+    assert st.z > p.Cav                                # at least one mirror bounce
+    assert st.puls_e < p.puls_e                        # the mirror loss was applied
+    assert rel(got, ref) < 1e-4
+
+
+def test_mirror_bounce_lens(gpu_lib):
+    import ctypes as C
+
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(bounce=BOUNCE_LENS, Ab_M=0.95)
+    ref = A.copy()
+    L = oracle.lib()
+    cd = C.POINTER(C.c_double)
+    L.or_mirror_lens.argtypes = [cd, C.c_int, C.c_int, C.c_int, cd, C.c_double, C.c_double]
+    r = np.ascontiguousarray(p.r, dtype=np.float64)
+    L.or_mirror_lens(oracle._p(ref.view(np.float64)), p.Nx, p.Ny, p.Nt, oracle._p(r), p.k0, p.roc)
+    with Propagator(p) as prop:
+        prop.upload(A)
+        prop.mirror_bounce(BOUNCE_LENS)
+        got = prop.download()
+        assert prop.state().puls_e == pytest.approx(p.puls_e * 0.95, rel=1e-12)
+    assert rel(got, ref) < 1e-5
