@@ -65,7 +65,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_driver(force)
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "driver", "mpc_run.c")
+DRIVER = os.path.join(os.path.dirname(LIB), "mpc_run")
+
+
+def build_driver(force: bool = False) -> str:
+    """The C run driver (driver/mpc_run.c), linked against the library beside it."""
+    hdr = os.path.join(HERE, "..", "include", "mpc_gpu.h")
+    if force or not _newer(DRIVER, [DRIVER_SRC, hdr, LIB]):
+        libdir = os.path.dirname(os.path.abspath(LIB))
+        libname = os.path.basename(LIB)
+        cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-Wall", "-Wextra", "-o", DRIVER, DRIVER_SRC,
+               f"-L{libdir}", f"-l:{libname}", "-Wl,-rpath,$ORIGIN", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -166,3 +166,47 @@ def sweep_cells(seed: int = 100, n: int = 64) -> list[CellConfig]:
         out.append(CellConfig(**shape, energy=energy, pressure=pressure, fwhm=fwhm, seed=seed + i,
                               passes=6, steps_per_pass=400))
     return out
+
+
+def write_run(cfg: CellConfig, datadir: str, nrun: int = 0) -> MPCParams:
+    """Write one cell's inputs in the reference's layout: datadir/datar.bin and datai.bin (the
+    seed field) and datadir%04d/param.bin (MPC.c:73-77, 159-168)."""
+    import os
+
+    from .params import write_field
+    p, A = make_cell(cfg)
+    run = f"{datadir}{nrun:04d}"
+    os.makedirs(run, exist_ok=True)
+    os.makedirs(datadir, exist_ok=True)
+    p.write(os.path.join(run, "param.bin"))
+    write_field(os.path.join(datadir, "datar.bin"), os.path.join(datadir, "datai.bin"), A)
+    return p
+
+
+def main(argv=None) -> int:
+    """python -m mpc_gb300.inputs --config 1 --datadir DIR [--nrun N] [--set key=value ...]"""
+    import argparse
+    ap = argparse.ArgumentParser(description="write param.bin, datar.bin and datai.bin for one cell")
+    ap.add_argument("--config", type=int, default=1, choices=[1, 2, 3])
+    ap.add_argument("--datadir", required=True, help="run directory prefix (the field goes here, "
+                                                     "param.bin into DATADIR%%04d)")
+    ap.add_argument("--nrun", type=int, default=0)
+    ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
+                    help="override a cell field, e.g. --set Nx=32 --set energy=1e-3")
+    a = ap.parse_args(argv)
+    kw = {}
+    for item in a.set:
+        k, v = item.split("=", 1)
+        if k not in CellConfig.__dataclass_fields__:
+            ap.error(f"unknown cell field {k}")
+        typ = type(getattr(CellConfig(), k))
+        kw[k] = typ(float(v)) if typ in (int, float) else typ(v)
+    cfg = {1: config1, 2: config2, 3: config3}[a.config](**kw)
+    p = write_run(cfg, a.datadir, a.nrun)
+    print(f"wrote {a.datadir}{a.nrun:04d}/param.bin and {a.datadir}/datar.bin, datai.bin: "
+          f"{p.Nx}x{p.Ny}x{p.Nt}, dist {p.dist} m, dzz {p.dzz} m")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
