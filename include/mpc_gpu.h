@@ -154,6 +154,24 @@ int mpc_energy(mpc_ctx *ctx, double *energy);
 /* Synchronise the context's stream; returns MPC_ERR_CUDA on an asynchronous fault. */
 int mpc_sync(mpc_ctx *ctx);
 
+/* ---- batches of independent cells (no counterpart in the reference) ----------------- */
+/* A batch runs one call on many contexts -- the cells of a parameter sweep, of any compiled
+ * grid shapes -- as one CUDA graph per call: each cell's launches are captured on the cell's
+ * stream (forked from and joined into the batch's stream) and the graph is launched once, so
+ * the cells' kernels overlap and the host issues one launch per call.  The contexts stay owned
+ * by the caller and must outlive the batch; each call waits for the cells' pending work first. */
+typedef struct mpc_batch mpc_batch;
+int mpc_batch_create(mpc_batch **batch, int n, mpc_ctx *const *cells);
+int mpc_batch_destroy(mpc_batch *batch);
+/* mpc_run_fixed(cell, nsteps) for every cell, as one graph. */
+int mpc_batch_run_fixed(mpc_batch *batch, int nsteps);
+/* One mpc_step_double attempt of every cell with state.z < dist, as one graph, then each
+ * cell's decision: bad[i] / err[i] as mpc_step_double returns them, bad[i] = -1 for cells
+ * that have finished.  bad and err hold n entries. */
+int mpc_batch_step_double(mpc_batch *batch, int *bad, double *err);
+/* Graphs launched and their total node count, since creation. */
+int mpc_batch_stats(mpc_batch *batch, long *graphs, long *nodes);
+
 /* ---- measurement and host buffers (no counterpart in the reference) ---------------- */
 /* Page-locked host buffer for fast host<->device copies of the field. */
 int mpc_host_alloc(void **ptr, size_t bytes);

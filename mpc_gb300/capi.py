@@ -74,6 +74,11 @@ SIGNATURES = {
     "mpc_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_kernel_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long), _dp, C.POINTER(C.c_long)]),
     "mpc_nonlinear_noalloc": (C.c_int, [C.POINTER(c_mpc_params), C.c_void_p, C.c_double, C.c_void_p]),
+    "mpc_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "mpc_batch_destroy": (C.c_int, [C.c_void_p]),
+    "mpc_batch_run_fixed": (C.c_int, [C.c_void_p, C.c_int]),
+    "mpc_batch_step_double": (C.c_int, [C.c_void_p, _ip, _dp]),
+    "mpc_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
 }
 
 _lib = None
@@ -290,6 +295,51 @@ class Propagator:
         _check(self.lib.mpc_kernel_times(self.h, C.byref(pm), C.byref(npn), C.byref(pl), C.byref(npl)),
                "mpc_kernel_times")
         return dict(pencil_ms=pm.value, n_pencil=npn.value, plane_ms=pl.value, n_plane=npl.value)
+
+
+class Batch:
+    """Many cells (Propagators, any grid shapes) run call by call as one CUDA graph each."""
+
+    def __init__(self, cells: list[Propagator]):
+        self.lib = load()
+        self.cells = list(cells)
+        arr = (C.c_void_p * len(self.cells))(*[c.h.value for c in self.cells])
+        h = C.c_void_p()
+        _check(self.lib.mpc_batch_create(C.byref(h), len(self.cells), arr), "mpc_batch_create")
+        self.h = h
+
+    def run_fixed(self, nsteps: int) -> None:
+        _check(self.lib.mpc_batch_run_fixed(self.h, int(nsteps)), "mpc_batch_run_fixed")
+
+    def step_double(self):
+        """One adaptive attempt of every unfinished cell: (bad[n], err[n]); bad = -1 when finished."""
+        n = len(self.cells)
+        bad = np.zeros(n, dtype=np.int32)
+        err = np.zeros(n)
+        _check(self.lib.mpc_batch_step_double(self.h, bad.ctypes.data_as(_ip), _ptr(err)), "mpc_batch_step_double")
+        return bad, err
+
+    def stats(self):
+        g, nn = C.c_long(0), C.c_long(0)
+        _check(self.lib.mpc_batch_stats(self.h, C.byref(g), C.byref(nn)), "mpc_batch_stats")
+        return dict(graphs=g.value, nodes=nn.value)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mpc_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PinnedArray:

@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -270,6 +271,9 @@ struct mpc_ctx {
     double2* io2 = nullptr;     // second complex128 staging (setStep)
     float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;  // packed twiddle tables
     float2 *C1 = nullptr, *C2 = nullptr;                    // step doubling (allocated on first use)
+    double* hsd = nullptr;   // pinned: error sums and C2's beam profiles of the last attempt (2 + Nx + Ny)
+    double sd_dz = 0.0;      // dz of the attempt in flight
+    int capturing = 0;       // launches are being captured into a CUDA graph (no synchronous calls)
     float* wpos = nullptr;
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
     std::vector<int> hfx, hfy, hft;
@@ -459,7 +463,7 @@ static int get_tables(mpc_ctx* c, double zd, double zp, double scale, TableSet* 
         *out = it->second;
         return MPC_OK;
     }
-    if (c->tables.size() > 64) {  // adaptive runs: recycle the cache
+    if (c->tables.size() > 64 && !c->capturing) {  // adaptive runs: recycle the cache
         cudaStreamSynchronize(c->st);
         for (auto& kv : c->tables) cudaFree(kv.second.f64);
         c->tables.clear();
@@ -542,6 +546,7 @@ int mpc_destroy(mpc_ctx* c) {
     prof_clear(c);
     for (auto& kv : c->tables) cudaFree(kv.second.f64);
     if (c->ident.f64) cudaFree(c->ident.f64);
+    if (c->hsd) cudaFreeHost(c->hsd);
     // only the base of each allocation: dfy/dft, dbetas/dr and lensy point inside dfx, dwr
     // and lensx, and cudaFree of an interior pointer fails and leaves an error pending in the
     // (process-wide) runtime for the caller's next CUDA call
@@ -1183,8 +1188,10 @@ int mpc_diag(mpc_ctx* c, double* temp, double* spec, double* BP1, double* BP2) {
     return MPC_OK;
 }
 
-int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err) {
-    if (!c || !bad || !err) return fail(MPC_ERR_ARG, "null argument");
+// Launch one step-doubling attempt on the context's stream, asynchronously: C1, C2, C2's beam
+// profiles, the error sums and the Richardson field, with the sums and profiles copied to the
+// pinned buffer hsd.  No synchronous call, so the launches can be captured into a graph.
+static int step_double_launch(mpc_ctx* c) {
     if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
     for (float2** b : {&c->C1, &c->C2})
         if (!*b && cudaMalloc(b, sizeof(float2) * c->N) != cudaSuccess) {
@@ -1192,8 +1199,14 @@ int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err)
             cudaGetLastError();
             return fail(MPC_ERR_NOMEM, "cudaMalloc step-doubling fields");
         }
+    if (!c->hsd && cudaMallocHost(&c->hsd, sizeof(double) * (2 + c->Nx + c->Ny)) != cudaSuccess) {
+        c->hsd = nullptr;
+        cudaGetLastError();
+        return fail(MPC_ERR_NOMEM, "cudaMallocHost step-doubling sums");
+    }
     mpc_state& st = c->state;
     const double dz = st.dzz, Cav = c->p.Cav;
+    c->sd_dz = dz;
     // calcexpR's sign logic (propagation.c:377-382), evaluated at the attempt's z for all three steps
     int signum = pass_sign(st.z, Cav);
     if (-st.signmem == signum) st.signmem = -st.signmem;
@@ -1229,13 +1242,21 @@ int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err)
     CK(cudaMemsetAsync(c->dred, 0, 2 * sizeof(double), c->st), "memset");
     k_richardson<<<c->nsm * 4, 256, 0, c->st>>>(c->C1, c->C2, c->C1, c->N, c->dred);
     CK(cudaGetLastError(), "k_richardson");
-    std::vector<double> h(2 + c->Nx + c->Ny);
-    CK(cudaMemcpyAsync(h.data(), c->dred, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->st), "D2H sums");
-    CK(cudaStreamSynchronize(c->st), "step_double");
-    mpc_calc1oes(h.data() + 2, c->Nx, c->r.data(), &st.bps1, st.y1);
-    mpc_calc1oes(h.data() + 2 + c->Nx, c->Ny, c->r.data(), &st.bps2, st.y2);
-    if (BP1) memcpy(BP1, h.data() + 2, sizeof(double) * c->Nx);
-    if (BP2) memcpy(BP2, h.data() + 2 + c->Nx, sizeof(double) * c->Ny);
+    c->launches += 3;
+    CK(cudaMemcpyAsync(c->hsd, c->dred, sizeof(double) * (2 + c->Nx + c->Ny), cudaMemcpyDeviceToHost, c->st),
+       "D2H sums");
+    return MPC_OK;
+}
+
+// Decide a launched attempt once its stream has completed: the setStep rule, acceptance
+// (pointer swap), z, mirror bounces crossed.
+static int step_double_finish(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err) {
+    mpc_state& st = c->state;
+    const double* h = c->hsd;
+    mpc_calc1oes(h + 2, c->Nx, c->r.data(), &st.bps1, st.y1);
+    mpc_calc1oes(h + 2 + c->Nx, c->Ny, c->r.data(), &st.bps2, st.y2);
+    if (BP1) memcpy(BP1, h + 2, sizeof(double) * c->Nx);
+    if (BP2) memcpy(BP2, h + 2 + c->Nx, sizeof(double) * c->Ny);
     *err = sqrt(h[0]) / sqrt(h[1]);
     st.err = *err;
     step_rule(*err, &st.dzz, c->p.def_err, c->p.dzmin, st.y1, st.y2, bad);
@@ -1244,14 +1265,143 @@ int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err)
     if (*bad) return MPC_OK;
     std::swap(c->S, c->C1);  // the accepted field (4 C2 - C1)/3
     const double z0 = st.z;
-    st.z = z0 + 2.0 * dz;    // A26: the step just taken
-    const int nb = bounces_between(z0, st.z, Cav);
+    st.z = z0 + 2.0 * c->sd_dz;  // A26: the step just taken
+    const int nb = bounces_between(z0, st.z, c->p.Cav);
+    int rc;
     for (int b = 0; b < nb; b++) {
         if (c->p.bounce_mode == MPC_BOUNCE_LENS && (rc = launch_plane(c, c->S, c->S, c->ident, &c->ident))) return rc;
         st.puls_e *= c->p.Ab_M;  // A24: the mirror loss the reference's bookkeeping never applies
     }
     if (st.z > c->p.dist) st.z = c->p.dist;
     st.nstep++;
+    return MPC_OK;
+}
+
+int mpc_step_double(mpc_ctx* c, double* BP1, double* BP2, int* bad, double* err) {
+    if (!c || !bad || !err) return fail(MPC_ERR_ARG, "null argument");
+    int rc = step_double_launch(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->st), "step_double");
+    return step_double_finish(c, BP1, BP2, bad, err);
+}
+
+// ---- batches of cells -------------------------------------------------------------------
+// A batch runs the same call on many independent contexts (cells of a sweep, of any grid
+// shapes) as one CUDA graph: the launches of every cell are captured on the cell's own stream,
+// forked from and joined into the batch's stream, and the graph is launched once, so kernels of
+// different cells overlap where one leaves SMs idle (tails, small grids) and the whole batch
+// costs one launch from the host.
+struct mpc_batch {
+    std::vector<mpc_ctx*> cells;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    long graphs = 0, nodes = 0;
+};
+
+int mpc_batch_create(mpc_batch** out, int n, mpc_ctx* const* cells) {
+    if (!out || n <= 0 || !cells) return fail(MPC_ERR_ARG, "null argument or empty batch");
+    *out = nullptr;
+    for (int i = 0; i < n; i++)
+        if (!cells[i]) return fail(MPC_ERR_ARG, "null context in batch");
+    mpc_batch* b = new mpc_batch();
+    b->cells.assign(cells, cells + n);
+    b->join.assign(n, nullptr);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        mpc_batch_destroy(b);
+        return fail(MPC_ERR_CUDA, "batch stream and events", e);
+    }
+    *out = b;
+    return MPC_OK;
+}
+
+int mpc_batch_destroy(mpc_batch* b) {
+    if (!b) return MPC_OK;
+    if (b->st) cudaStreamSynchronize(b->st);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return MPC_OK;
+}
+
+// Capture per_cell(cell) for every active cell into one graph and run it to completion.
+static int batch_graph(mpc_batch* b, const std::vector<char>& active, const std::function<int(mpc_ctx*)>& per_cell) {
+    for (size_t i = 0; i < b->cells.size(); i++)
+        if (active[i]) CK(cudaStreamSynchronize(b->cells[i]->st), "batch: cell stream");
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeRelaxed), "begin graph capture");
+    int rc = MPC_OK;
+    cudaError_t e = cudaEventRecord(b->fork, b->st);
+    for (size_t i = 0; i < b->cells.size() && rc == MPC_OK && e == cudaSuccess; i++) {
+        if (!active[i]) continue;
+        mpc_ctx* c = b->cells[i];
+        e = cudaStreamWaitEvent(c->st, b->fork, 0);
+        if (e != cudaSuccess) break;
+        c->capturing = 1;
+        rc = per_cell(c);
+        c->capturing = 0;
+        if (rc == MPC_OK) e = cudaEventRecord(b->join[i], c->st);
+        if (rc == MPC_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[i], 0);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e_end = cudaStreamEndCapture(b->st, &g);
+    if (rc != MPC_OK || e != cudaSuccess || e_end != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (rc != MPC_OK) return rc;
+        return fail(MPC_ERR_CUDA, "batch graph capture", e != cudaSuccess ? e : e_end);
+    }
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    size_t nn = 0;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &nn);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (ge) cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(MPC_ERR_CUDA, "batch graph", e);
+    b->graphs++;
+    b->nodes += (long)nn;
+    return MPC_OK;
+}
+
+int mpc_batch_run_fixed(mpc_batch* b, int nsteps) {
+    if (!b) return fail(MPC_ERR_ARG, "null batch");
+    std::vector<char> active(b->cells.size(), 1);
+    for (size_t i = 0; i < b->cells.size(); i++)
+        if (!b->cells[i]->have_field) return fail(MPC_ERR_STATE, "a cell of the batch has no field");
+    return batch_graph(b, active, [nsteps](mpc_ctx* c) { return mpc_run_fixed(c, nsteps); });
+}
+
+int mpc_batch_step_double(mpc_batch* b, int* bad, double* err) {
+    if (!b || !bad || !err) return fail(MPC_ERR_ARG, "null argument");
+    const size_t n = b->cells.size();
+    std::vector<char> active(n, 0);
+    int any = 0;
+    for (size_t i = 0; i < n; i++) {
+        mpc_ctx* c = b->cells[i];
+        if (!c->have_field) return fail(MPC_ERR_STATE, "a cell of the batch has no field");
+        active[i] = c->state.z < c->p.dist;
+        any |= active[i];
+        bad[i] = -1;
+        err[i] = 0.0;
+    }
+    if (!any) return MPC_OK;
+    int rc = batch_graph(b, active, [](mpc_ctx* c) { return step_double_launch(c); });
+    if (rc) return rc;
+    for (size_t i = 0; i < n; i++)
+        if (active[i] && (rc = step_double_finish(b->cells[i], nullptr, nullptr, &bad[i], &err[i]))) return rc;
+    return MPC_OK;
+}
+
+int mpc_batch_stats(mpc_batch* b, long* graphs, long* nodes) {
+    if (!b || !graphs || !nodes) return fail(MPC_ERR_ARG, "null argument");
+    *graphs = b->graphs;
+    *nodes = b->nodes;
     return MPC_OK;
 }
 

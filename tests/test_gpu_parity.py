@@ -58,19 +58,36 @@ def test_calcexpR(gpu_lib):
             assert np.abs(got - ref).max() < 2e-7
 
 
-def test_ADK_fp64(gpu_lib):
+GASES = ["Argon", "Helium", "Neon", "Air", "Nitrogen", "Xenon", "Krypton"]
+
+
+@pytest.mark.parametrize("gas", GASES)
+def test_ADK_fp64(gpu_lib, gas):
+    """ADK rates of both stages on the device (FP64) for every gas of plasma.c:4-115."""
     from mpc_gb300.capi import Propagator
-    p, A, o = small_cell()
+    p, A, o = small_cell(gas=gas)
     E = np.geomspace(1e-4, 0.5, 257)
     with Propagator(p) as prop:
         r1, r2 = prop.ADK(E)
-    I1, I2 = oracle.ionizpot("Argon")
+    I1, I2 = oracle.ionizpot(gas)
     Iion = np.array([I1, I2]) / 27.21
     nq = np.array([1 / np.sqrt(2 * Iion[0]), 2 / np.sqrt(2 * Iion[1])])
     from math import gamma
     Cnl = np.array([np.sqrt(2 ** (2 * n) / (n * gamma(n + 1) * gamma(n))) for n in nq])
     e1, e2 = oracle.ADK(E, Cnl, [1, 1], nq, [0, 0], Iion)
     assert rel(r1, e1) < 1e-12 and rel(r2, e2) < 1e-12
+
+
+@pytest.mark.parametrize("gas", GASES)
+def test_ioniz_every_gas(gpu_lib, gas):
+    """Free-electron density and collision time of every gas (ionization potentials, atom
+    densities and cross-sections of plasma.c:4-115) against the oracle."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(gas=gas, energy=3e-3, fwhm=100e-15, pressure=2.0, beam_w=0.3e-3)
+    tau, fe = o.ioniz(A)
+    with Propagator(p) as prop:
+        t_g, f_g = prop.ioniz(A)
+    assert rel(t_g, tau) < 1e-5 and fe.max() > 0 and rel(f_g, fe) < 1e-4
 
 
 def test_ioniz(gpu_lib):
