@@ -137,6 +137,68 @@ int mpc_run_fixed(mpc_ctx *ctx, int nsteps);
  * y1, y2, bps1, bps2 are updated from them; attempts += 1. */
 int mpc_step_double(mpc_ctx *ctx, double *BP1, double *BP2, int *bad, double *err);
 
+/* One split step L(dzz/2) N(dzz) L(dzz/2) of any length on the device-resident field at
+ * state.z (the device form of ssfmprop, propagation.c:111-372, with the diffraction sign of
+ * calcexpR): state.z += dzz, mirror planes crossed apply a bounce as in mpc_step_double. */
+int mpc_step(mpc_ctx *ctx, double dzz);
+
+/* ---- learned step-size control (no counterpart in the reference) -------------------- */
+/* Running maxima over the split steps since the last reset: {peak intensity [W/m^2], peak
+ * ionization fraction, peak nonlinear phase rate |Im A_nl| [rad/m], peak amplitude rate
+ * |Re A_nl| [1/m]}, gathered inside the pencil sweep; reset != 0 restarts them. */
+int mpc_step_stats(mpc_ctx *ctx, float out[4], int reset);
+#define MPC_NFEATURES 16
+/* The step-size controller's 16 features of the device field and state (one reduction pass
+ * over the field plus the step statistics): log10 peak intensity, log10 peak ionization, log10
+ * phase rate, log10 amplitude rate, log10 energy, spectral rms width and centroid shift (% of
+ * w0), beam rms widths x, y (/ window), log10(dzz/Cav), position within the pass, log10 field
+ * peakiness, log10 density - 25, log10 phase per step at dzz, plasma flag, self-steepening flag. */
+int mpc_features(mpc_ctx *ctx, float f[MPC_NFEATURES]);
+
+/* The network of the learned controller: 16 features -> 64 -> 64 -> 1 (SiLU), predicting
+ * log(dz / Cav) of the next step.  Weights are MPC_MLP_NWEIGHTS floats packed as W1[64][16],
+ * b1[64], W2[64][64], b2[64], W3[64], b3; inputs are normalised as (x - mean) / std and the
+ * output de-normalised as y_mean + y_std * out.  Training and inference run in this
+ * library's own kernels on the GPU (minibatch Adam on the mean squared error in normalised
+ * units).  Host arrays throughout: X is n x 16 row-major, y has n entries. */
+#define MPC_MLP_NWEIGHTS 5313
+typedef struct mpc_mlp mpc_mlp;
+int mpc_mlp_num_weights(void);
+int mpc_mlp_create(mpc_mlp **mlp, unsigned long long seed);   /* uniform(+-1/sqrt(fan_in)) init */
+int mpc_mlp_destroy(mpc_mlp *mlp);
+int mpc_mlp_set_normalization(mpc_mlp *mlp, const float mean[MPC_NFEATURES], const float stdv[MPC_NFEATURES],
+                              float y_mean, float y_std);
+/* out = {mean[16], std[16], y_mean, y_std} */
+int mpc_mlp_get_normalization(mpc_mlp *mlp, float out[2 * MPC_NFEATURES + 2]);
+int mpc_mlp_get_weights(mpc_mlp *mlp, float *w);
+int mpc_mlp_set_weights(mpc_mlp *mlp, const float *w);      /* also restarts Adam */
+/* Mean squared error (normalised units) over all n samples and its gradient w.r.t. the weights. */
+int mpc_mlp_loss_grad(mpc_mlp *mlp, const float *X, const float *y, int n, float *grad, float *loss);
+/* epochs of minibatch Adam (lr, beta 0.9 / 0.999), a Fisher-Yates shuffle per epoch from seed;
+ * final_loss = the last epoch's mean loss. */
+int mpc_mlp_train(mpc_mlp *mlp, const float *X, const float *y, int n, int epochs, int batch, float lr,
+                  unsigned long long seed, float *final_loss);
+int mpc_mlp_predict(mpc_mlp *mlp, const float *X, int n, float *y);
+/* One sample, without allocating (the controller's per-step call). */
+int mpc_mlp_predict1(mpc_mlp *mlp, const float x[MPC_NFEATURES], float *y);
+
+/* The learned controller (run to state.z = dist): plain split steps (mpc_step) of
+ * dz = safety * Cav * exp(network(features)), capped at twice the previous step, quantised
+ * down to 16 steps per octave of Cav and shortened to land on the next mirror plane; the run opens with one step-doubling attempt, and every
+ * check_every steps the step is taken as a step-doubling attempt instead, whose error checks
+ * the network: above def_err, the next fallback_len accepted steps are plain step doubling
+ * (mpc_step_double) before the network is used again. */
+typedef struct {
+    int steps;              /* plain steps at the network's dz */
+    int checks;             /* periodic step-doubling checks */
+    int check_failures;     /* checks whose error exceeded def_err (each starts a fallback) */
+    int fallback_attempts;  /* step-doubling attempts outside the checks */
+    long executed_steps;    /* split steps executed (3 per step-doubling attempt) */
+    double dz_min, dz_max;  /* range of the network's steps [m] */
+} mpc_learned_stats;
+int mpc_run_learned(mpc_ctx *ctx, mpc_mlp *mlp, double safety, int check_every, int fallback_len,
+                    mpc_learned_stats *out);
+
 /* One mirror bounce of the device-resident field, now: MPC_BOUNCE_LENS multiplies it by the
  * mirror's focusing phase exp(-i k0 (x^2 + y^2) / roc); MPC_BOUNCE_SIGNFLIP flips
  * state.signmem, the reference's bookkeeping of a bounce (propagation.c:334-341; the

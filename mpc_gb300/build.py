@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.environ.get("MPC_GPU_OBJ_DIR", os.path.join(HERE, "_build"))
 LIB = os.environ.get("MPC_GPU_LIB_OUT", os.path.join(HERE, "libmpc_gpu.so"))
 SOURCES = ["mpc_capi.cu", "mpc_shapes_a.cu", "mpc_shapes_b.cu", "mpc_shapes_c.cu", "mpc_shapes_d.cu",
-           "mpc_noalloc.cu"]
+           "mpc_noalloc.cu", "mpc_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
 # extra defines for tuning builds, e.g. MPC_NVCC_EXTRA="-DMPC_PREFETCH=0"

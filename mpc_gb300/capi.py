@@ -22,6 +22,7 @@ ERRORS = {1: "MPC_ERR_ARG", 2: "MPC_ERR_SHAPE", 3: "MPC_ERR_CUDA", 4: "MPC_ERR_N
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
 
 
 class c_mpc_params(C.Structure):
@@ -79,7 +80,31 @@ SIGNATURES = {
     "mpc_batch_run_fixed": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_batch_step_double": (C.c_int, [C.c_void_p, _ip, _dp]),
     "mpc_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "mpc_step": (C.c_int, [C.c_void_p, C.c_double]),
+    "mpc_step_stats": (C.c_int, [C.c_void_p, _fp, C.c_int]),
+    "mpc_features": (C.c_int, [C.c_void_p, _fp]),
+    "mpc_mlp_num_weights": (C.c_int, []),
+    "mpc_mlp_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_ulonglong]),
+    "mpc_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "mpc_mlp_set_normalization": (C.c_int, [C.c_void_p, _fp, _fp, C.c_float, C.c_float]),
+    "mpc_mlp_get_normalization": (C.c_int, [C.c_void_p, _fp]),
+    "mpc_mlp_get_weights": (C.c_int, [C.c_void_p, _fp]),
+    "mpc_mlp_set_weights": (C.c_int, [C.c_void_p, _fp]),
+    "mpc_mlp_loss_grad": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int, _fp, _fp]),
+    "mpc_mlp_train": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _fp]),
+    "mpc_mlp_predict": (C.c_int, [C.c_void_p, _fp, C.c_int, _fp]),
+    "mpc_mlp_predict1": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "mpc_run_learned": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_void_p]),
 }
+
+_fp = C.POINTER(C.c_float)
+NFEATURES = 16
+
+
+class c_mpc_learned_stats(C.Structure):
+    _fields_ = [("steps", C.c_int), ("checks", C.c_int), ("check_failures", C.c_int),
+                ("fallback_attempts", C.c_int), ("executed_steps", C.c_long), ("dz_min", C.c_double),
+                ("dz_max", C.c_double)]
 
 _lib = None
 
@@ -251,6 +276,26 @@ class Propagator:
             out.update(BP1=BP1, BP2=BP2)
         return out
 
+    def step(self, dzz: float) -> None:
+        """One split step of length dzz on the device field at state.z (mirror bounces crossed applied)."""
+        _check(self.lib.mpc_step(self.h, float(dzz)), "mpc_step")
+
+    def step_stats(self, reset: bool = False) -> np.ndarray:
+        out = np.zeros(4, dtype=np.float32)
+        _check(self.lib.mpc_step_stats(self.h, out.ctypes.data_as(_fp), int(reset)), "mpc_step_stats")
+        return out
+
+    def features(self) -> np.ndarray:
+        f = np.zeros(NFEATURES, dtype=np.float32)
+        _check(self.lib.mpc_features(self.h, f.ctypes.data_as(_fp)), "mpc_features")
+        return f
+
+    def run_learned(self, mlp: "MLP", safety: float = 0.9, check_every: int = 8, fallback_len: int = 4) -> dict:
+        st = c_mpc_learned_stats()
+        _check(self.lib.mpc_run_learned(self.h, mlp.h, float(safety), int(check_every), int(fallback_len), C.byref(st)),
+               "mpc_run_learned")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
     def mirror_bounce(self, mode: int) -> None:
         _check(self.lib.mpc_mirror_bounce(self.h, int(mode)), "mpc_mirror_bounce")
 
@@ -295,6 +340,79 @@ class Propagator:
         _check(self.lib.mpc_kernel_times(self.h, C.byref(pm), C.byref(npn), C.byref(pl), C.byref(npl)),
                "mpc_kernel_times")
         return dict(pencil_ms=pm.value, n_pencil=npn.value, plane_ms=pl.value, n_plane=npl.value)
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+class MLP:
+    """The learned controller's network (16 -> 64 -> 64 -> 1, SiLU) on the GPU."""
+
+    def __init__(self, seed: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        _check(self.lib.mpc_mlp_create(C.byref(h), C.c_ulonglong(seed)), "mpc_mlp_create")
+        self.h = h
+        self.nw = int(self.lib.mpc_mlp_num_weights())
+
+    def set_normalization(self, mean, std, y_mean: float, y_std: float) -> None:
+        m, s = _f32(mean, (NFEATURES,)), _f32(std, (NFEATURES,))
+        _check(self.lib.mpc_mlp_set_normalization(self.h, m.ctypes.data_as(_fp), s.ctypes.data_as(_fp),
+                                                  float(y_mean), float(y_std)), "mpc_mlp_set_normalization")
+
+    def normalization(self) -> np.ndarray:
+        out = np.zeros(2 * NFEATURES + 2, dtype=np.float32)
+        _check(self.lib.mpc_mlp_get_normalization(self.h, out.ctypes.data_as(_fp)), "mpc_mlp_get_normalization")
+        return out
+
+    @property
+    def weights(self) -> np.ndarray:
+        w = np.zeros(self.nw, dtype=np.float32)
+        _check(self.lib.mpc_mlp_get_weights(self.h, w.ctypes.data_as(_fp)), "mpc_mlp_get_weights")
+        return w
+
+    @weights.setter
+    def weights(self, w) -> None:
+        w = _f32(w, (self.nw,))
+        _check(self.lib.mpc_mlp_set_weights(self.h, w.ctypes.data_as(_fp)), "mpc_mlp_set_weights")
+
+    def loss_grad(self, X, y):
+        X, y = _f32(X), _f32(y)
+        g = np.zeros(self.nw, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(self.lib.mpc_mlp_loss_grad(self.h, X.ctypes.data_as(_fp), y.ctypes.data_as(_fp), len(y),
+                                          g.ctypes.data_as(_fp), loss.ctypes.data_as(_fp)), "mpc_mlp_loss_grad")
+        return float(loss[0]), g
+
+    def train(self, X, y, epochs: int = 20, batch: int = 256, lr: float = 1e-3, seed: int = 0) -> float:
+        X, y = _f32(X), _f32(y)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(self.lib.mpc_mlp_train(self.h, X.ctypes.data_as(_fp), y.ctypes.data_as(_fp), len(y), int(epochs),
+                                      int(batch), float(lr), C.c_ulonglong(seed), loss.ctypes.data_as(_fp)),
+               "mpc_mlp_train")
+        return float(loss[0])
+
+    def predict(self, X) -> np.ndarray:
+        X = _f32(X)
+        y = np.zeros(len(X), dtype=np.float32)
+        _check(self.lib.mpc_mlp_predict(self.h, X.ctypes.data_as(_fp), len(X), y.ctypes.data_as(_fp)),
+               "mpc_mlp_predict")
+        return y
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mpc_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Batch:

@@ -200,6 +200,39 @@ __global__ void k_pencil_energy_slots(const float2* __restrict__ S, int NP, int 
     E[q] = acc * scale;
 }
 
+// Moments of the field S (slot layout) for the step-size features, FP64 across threads:
+// out = {sum |S|^2, sum w|S|^2, sum w^2|S|^2, sum x|S|^2, sum x^2|S|^2, sum y|S|^2, sum y^2|S|^2}
+// (w = omega offset of the slot, x, y = transverse positions) and mx = max |S|^2 (bit pattern).
+__global__ void k_moments(const float2* __restrict__ S, long N, int NP, int Nx, int SLO, const float* __restrict__ wpos,
+                          const double* __restrict__ r, double* out, unsigned int* mx) {
+    __shared__ double sh[32];
+    double m[7] = {0, 0, 0, 0, 0, 0, 0};
+    float vmax = 0.0f;
+    const long blk = (long)NP * SLO;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+        const float2 v = S[i];
+        const float e = fmaf(v.x, v.x, v.y * v.y);
+        const long rem = i % blk;
+        const int q = (int)(rem / SLO);
+        const int slot = (int)(i / blk) * SLO + (int)(rem % SLO);
+        const double w = wpos[slot], x = r[q % Nx], y = r[q / Nx];
+        m[0] += e;
+        m[1] += w * e;
+        m[2] += w * w * e;
+        m[3] += x * e;
+        m[4] += x * x * e;
+        m[5] += y * e;
+        m[6] += y * y * e;
+        vmax = fmaxf(vmax, e);
+    }
+    for (int k = 0; k < 7; k++) {
+        const double t = block_sum(m[k], sh);
+        if (threadIdx.x == 0) atomicAdd(out + k, t);
+    }
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, __float_as_uint(vmax));
+}
+
 // spec[freq(pos)] = scale * sum_q |S[pos, q]|^2 for the slot layout; one block per slot
 __global__ void k_spec(const float2* __restrict__ S, int NP, int SLO, const int* ft, double scale, double* spec) {
     __shared__ double sh[32];
@@ -272,6 +305,8 @@ struct mpc_ctx {
     float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;  // packed twiddle tables
     float2 *C1 = nullptr, *C2 = nullptr;                    // step doubling (allocated on first use)
     double* hsd = nullptr;   // pinned: error sums and C2's beam profiles of the last attempt (2 + Nx + Ny)
+    unsigned int* dstats = nullptr;  // running maxima of the split steps since the last reset (4)
+    double* dmom = nullptr;          // field moments (7 doubles) and max |S|^2 (bits, after them)
     double sd_dz = 0.0;      // dz of the attempt in flight
     int capturing = 0;       // launches are being captured into a CUDA graph (no synchronous calls)
     float* wpos = nullptr;
@@ -551,7 +586,8 @@ int mpc_destroy(mpc_ctx* c) {
     // and lensx, and cudaFree of an interior pointer fails and leaves an error pending in the
     // (process-wide) runtime for the caller's next CUDA call
     void* ptrs[] = {c->S,   c->scratch, c->io,  c->io2,     c->twx,    c->twy,  c->twt,
-                    c->wpos, c->dfx,    c->dwr, c->lensx,   c->penergy, c->dred, c->C1, c->C2};
+                    c->wpos, c->dfx,    c->dwr, c->lensx,   c->penergy, c->dred, c->C1, c->C2,
+                    c->dstats, c->dmom};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->st) cudaStreamDestroy(c->st);
@@ -671,6 +707,9 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
     TRYC(cudaMalloc(&c->penergy, sizeof(double) * c->NP), "cudaMalloc pencil energies");
     // reductions: temp [0, Nt), spec [Nt, 2 Nt), beam profiles and sums use the front
     TRYC(cudaMalloc(&c->dred, sizeof(double) * (2 * Nt + Nx + Ny + 64)), "cudaMalloc reductions");
+    TRYC(cudaMalloc(&c->dstats, 4 * sizeof(unsigned int)), "cudaMalloc step statistics");
+    TRYC(cudaMemsetAsync(c->dstats, 0, 4 * sizeof(unsigned int), c->st), "memset step statistics");
+    TRYC(cudaMalloc(&c->dmom, 8 * sizeof(double)), "cudaMalloc field moments");
     {
         TRY(alloc_tables(c, &c->ident));
         TabIn in{c->dwr, c->dbetas, c->dfx, c->dfy, c->dft, Nx, Ny, Nt, 0.0, 0.0, p->k0, p->alpha,
@@ -863,6 +902,7 @@ static int pencil_step(mpc_ctx* c, double dz, float2* buf = nullptr) {
     PencilArgs a{};
     a.in = buf ? buf : c->S;
     a.out = buf ? buf : c->S;
+    a.stats = c->dstats;
     a.nl = c->nl;
     a.nl.dz = (float)dz;
     return launch_pencil(c, mpc::PM_STEP, a);
@@ -1402,6 +1442,158 @@ int mpc_batch_stats(mpc_batch* b, long* graphs, long* nodes) {
     if (!b || !graphs || !nodes) return fail(MPC_ERR_ARG, "null argument");
     *graphs = b->graphs;
     *nodes = b->nodes;
+    return MPC_OK;
+}
+
+int mpc_step(mpc_ctx* c, double dzz) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    if (!(dzz > 0)) return fail(MPC_ERR_ARG, "dzz must be positive");
+    mpc_state& st = c->state;
+    int signum = pass_sign(st.z, c->p.Cav);  // calcexpR (propagation.c:377-382)
+    if (-st.signmem == signum) st.signmem = -st.signmem;
+    if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
+    const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
+    TableSet t1, t2;
+    int rc;
+    if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sNP, &t1))) return rc;
+    if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sN, &t2))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
+    if ((rc = pencil_step(c, dzz))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t2, nullptr))) return rc;
+    const double z0 = st.z;
+    st.z = z0 + dzz;
+    const int nb = bounces_between(z0, st.z, c->p.Cav);
+    for (int b = 0; b < nb; b++) {
+        if (c->p.bounce_mode == MPC_BOUNCE_LENS && (rc = launch_plane(c, c->S, c->S, c->ident, &c->ident))) return rc;
+        st.puls_e *= c->p.Ab_M;
+    }
+    if (st.z > c->p.dist) st.z = c->p.dist;
+    st.nstep++;
+    return MPC_OK;
+}
+
+int mpc_step_stats(mpc_ctx* c, float* out, int reset) {
+    if (!c || !out) return fail(MPC_ERR_ARG, "null argument");
+    unsigned int u[4];
+    CK(cudaMemcpyAsync(u, c->dstats, sizeof u, cudaMemcpyDeviceToHost, c->st), "D2H step statistics");
+    if (reset) CK(cudaMemsetAsync(c->dstats, 0, sizeof u, c->st), "reset step statistics");
+    CK(cudaStreamSynchronize(c->st), "step statistics");
+    for (int k = 0; k < 4; k++) memcpy(&out[k], &u[k], sizeof(float));
+    // device units -> physical: |a|^2 -> intensity [W/m^2]
+    out[0] = (float)((double)out[0] * I_UNIT);
+    return MPC_OK;
+}
+
+int mpc_features(mpc_ctx* c, float* f) {
+    if (!c || !f) return fail(MPC_ERR_ARG, "null argument");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    float stt[4];
+    int rc = mpc_step_stats(c, stt, 0);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->dmom, 0, 8 * sizeof(double), c->st), "memset moments");
+    k_moments<<<c->nsm * 4, 256, 0, c->st>>>(c->S, c->N, (int)c->NP, c->Nx, c->ops->SLO, c->wpos, c->dr, c->dmom,
+                                            reinterpret_cast<unsigned int*>(c->dmom + 7));
+    CK(cudaGetLastError(), "k_moments");
+    c->launches++;
+    double m[8];
+    CK(cudaMemcpyAsync(m, c->dmom, sizeof m, cudaMemcpyDeviceToHost, c->st), "D2H moments");
+    CK(cudaStreamSynchronize(c->st), "features");
+    float smax;
+    memcpy(&smax, &m[7], sizeof smax);
+    const mpc_params& p = c->p;
+    const mpc_state& st = c->state;
+    const double E = m[0] > 0 ? m[0] : 1e-300;
+    const double wm = m[1] / E, ws = sqrt(fmax(m[2] / E - wm * wm, 0.0));
+    const double xm = m[3] / E, xs = sqrt(fmax(m[4] / E - xm * xm, 0.0));
+    const double ym = m[5] / E, ys = sqrt(fmax(m[6] / E - ym * ym, 0.0));
+    const double window = c->Nx * p.dr;
+    const double energy = m[0] * (double)c->Nt / (c->fs * c->fs) * p.dr * p.dr * p.deltat * HBAR * p.w0;
+    const double zc = st.z / p.Cav;
+    const double v[16] = {
+        log10(1e-30 + stt[0]),                          // peak intensity of the last steps [W/m^2]
+        log10(1e-12 + stt[1]),                          // peak ionization fraction
+        log10(1e-12 + stt[2]),                          // peak nonlinear phase rate [rad/m]
+        log10(1e-12 + stt[3]),                          // peak amplitude rate [1/m]
+        log10(1e-30 + energy),                          // pulse energy [J]
+        ws / p.w0 * 1e2,                                // spectral rms width / w0 [%]
+        wm / p.w0 * 1e2,                                // spectral centroid shift / w0 [%]
+        xs / window,                                    // beam rms width x / window
+        ys / window,                                    // beam rms width y / window
+        log10(st.dzz / p.Cav),                          // current step / mirror separation
+        zc - floor(zc),                                 // position within the pass
+        log10(1e-30 + (double)smax / E),                // spectral-spatial peakiness
+        log10(1e-30 + p.rho_nt) - 25.0,                 // neutral density
+        log10(1e-12 + stt[2] * st.dzz),                 // nonlinear phase per step at the current dz
+        (double)(p.plasm == 1),                         // plasma terms on
+        (double)(p.sst_on == 1),                        // self-steepening on
+    };
+    for (int k = 0; k < 16; k++) f[k] = (float)v[k];
+    return MPC_OK;
+}
+
+int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, int fallback_len,
+                    mpc_learned_stats* out) {
+    if (!c || !mlp || !out || !(safety > 0) || check_every < 1 || fallback_len < 0)
+        return fail(MPC_ERR_ARG, "bad argument");
+    if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
+    memset(out, 0, sizeof *out);
+    mpc_state& st = c->state;
+    const double Cav = c->p.Cav, dist = c->p.dist, dzmin = c->p.dzmin;
+    int rc, bad;
+    double err;
+    float f[MPC_NFEATURES], stt[4];
+    int fb = 1;  // open with one step-doubling attempt (it also provides the first statistics)
+    int since_check = 0;
+    double dz_last = st.dzz;
+    while (st.z < dist * (1.0 - 1e-12)) {
+        if (fb > 0) {
+            const double h = st.dzz;
+            if ((rc = mpc_step_double(c, nullptr, nullptr, &bad, &err))) return rc;
+            out->fallback_attempts++;
+            out->executed_steps += 3;
+            if (!bad) {
+                fb--;
+                dz_last = 2.0 * h;
+            }
+            continue;
+        }
+        if ((rc = mpc_features(c, f))) return rc;
+        if ((rc = mpc_step_stats(c, stt, 1))) return rc;
+        float y = 0.0f;
+        if ((rc = mpc_mlp_predict1(mlp, f, &y))) return fail(rc, "network prediction failed");
+        double dz = safety * Cav * exp((double)y);
+        if (!(dz > 0) || !isfinite(dz)) dz = dz_last;
+        dz = fmin(dz, 2.0 * dz_last);
+        dz = Cav * exp2(floor(16.0 * log2(dz / Cav)) / 16.0);   // cached phase tables stay few
+        dz = fmax(dz, dzmin);
+        // land on the next mirror plane rather than step across it, so each bounce is applied
+        // where the mirror is
+        const double next_plane = (floor(st.z / Cav + 1e-9) + 1.0) * Cav;
+        if (next_plane - st.z > 1e-9 * Cav) dz = fmin(dz, next_plane - st.z);
+        dz = fmin(dz, dist - st.z);
+        if (++since_check >= check_every) {
+            since_check = 0;
+            out->checks++;
+            st.dzz = dz / 2.0;
+            if ((rc = mpc_step_double(c, nullptr, nullptr, &bad, &err))) return rc;
+            out->executed_steps += 3;
+            if (bad || err > c->p.def_err) {
+                out->check_failures++;
+                fb = fallback_len;
+            } else {
+                dz_last = dz;
+            }
+            continue;
+        }
+        if ((rc = mpc_step(c, dz))) return rc;
+        out->steps++;
+        out->executed_steps++;
+        out->dz_min = out->steps == 1 ? dz : fmin(out->dz_min, dz);
+        out->dz_max = fmax(out->dz_max, dz);
+        dz_last = dz;
+        st.dzz = dz;
+    }
     return MPC_OK;
 }
 

@@ -91,6 +91,7 @@ struct PencilArgs {
     double* temp;            // TEMP: sum_xy |out|^2 per t, Nt (accumulated)
     double* tau_out;         // IONIZ: tau_c, reference layout
     double* fe_out;          // IONIZ: freeelectrons_sp, reference layout
+    unsigned int* stats;     // STEP: running maxima of the step (nonlinear_tile), or null
     double in_scale;         // ENTRY: input multiplier (to device units, includes 1/Nt)
     double out_scale;        // EXIT/TEMP: output multiplier (from device units)
     int NP;                  // Nx * Ny
@@ -248,11 +249,12 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
 // IONIZ_ONLY = false: A *= exp(dz * A_nl) in place (propagation.c:244-327 with the A13/A14
 // fixes).  IONIZ_ONLY = true: write tau_c and freeelectrons_sp (plasma.c:118-245 outputs)
 // in the reference layout instead, A untouched.  Thread (p = tid % P, ch = tid / P) walks
-// the 32 samples t = 32 ch .. 32 ch + 31 of pencil p.
+// the 32 samples t = 32 ch .. 32 ch + 31 of pencil p.  The step's running maxima go to `mx`:
+// {|a|^2 (device units), ionization fraction, |Im A_nl| (phase rate, rad/m), |Re A_nl| (1/m)}.
 template <int NT, int P, bool IONIZ_ONLY>
 __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restrict__ scr, const NLConst& c,
                                                void* scan_mem, int tid, double* tau_out, double* fe_out,
-                                               int q0, int NP) {
+                                               int q0, int NP, float4& mx) {
     using V = PencilView<NT, P>;
     constexpr int TPP = NT / 32;
     const int p = tid % P;
@@ -328,8 +330,9 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
                 continue;
             }
             const float pl = c.rho_half * ions;
+            const float a2 = fmaf(a.x, a.x, a.y * a.y);
             float re = -pl * ip.sigma;
-            float im = fmaf(c.gam, fmaf(a.x, a.x, a.y * a.y), -pl * ip.qw);
+            float im = fmaf(c.gam, a2, -pl * ip.qw);
             if (c.sst_c != 0.0f) {
                 const float2 sd = cmulc(dA[i * P], a);  // dA * conj(A)
                 re = fmaf(-3.0f * c.sst_c, sd.x, re);
@@ -339,13 +342,15 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float sn, cs;
             sincos_small(c.dz * im, &sn, &cs);
             w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
+            mx = make_float4(fmaxf(mx.x, a2), fmaxf(mx.y, ions), fmaxf(mx.z, fabsf(im)), fmaxf(mx.w, fabsf(re)));
         }
     } else {
 #pragma unroll 4
         for (int i = 0; i < 32; i++) {
             const float2 a = w[V::walk(i)];
+            const float a2 = fmaf(a.x, a.x, a.y * a.y);
             float re = 0.0f;
-            float im = c.gam * fmaf(a.x, a.x, a.y * a.y);
+            float im = c.gam * a2;
             if (c.sst_c != 0.0f) {
                 const float2 sd = cmulc(dA[i * P], a);
                 re = -3.0f * c.sst_c * sd.x;
@@ -355,7 +360,28 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float sn, cs;
             sincos_small(c.dz * im, &sn, &cs);
             w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
+            mx = make_float4(fmaxf(mx.x, a2), mx.y, fmaxf(mx.z, fabsf(im)), fmaxf(mx.w, fabsf(re)));
         }
+    }
+}
+
+// Block-wide maximum of each component of v into stats[0..3] (non-negative floats, whose
+// bit patterns order like the values); one atomic per component and CTA.
+template <int TH>
+__device__ __forceinline__ void stats_max(float4 v, unsigned int* stats, float* red, int tid) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x = fmaxf(v.x, __shfl_xor_sync(0xffffffffu, v.x, o));
+        v.y = fmaxf(v.y, __shfl_xor_sync(0xffffffffu, v.y, o));
+        v.z = fmaxf(v.z, __shfl_xor_sync(0xffffffffu, v.z, o));
+        v.w = fmaxf(v.w, __shfl_xor_sync(0xffffffffu, v.w, o));
+    }
+    if ((tid & 31) == 0) reinterpret_cast<float4*>(red)[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 4) {
+        float m = 0.0f;
+        for (int w = 0; w < TH / 32; w++) m = fmaxf(m, red[4 * w + tid]);
+        atomicMax(&stats[tid], __float_as_uint(m));
     }
 }
 
@@ -475,6 +501,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
         for (int t = tid; t < NT; t += TH) tsum[t] = 0.0;
         __syncthreads();
     }
+    float4 mx = make_float4(0.f, 0.f, 0.f, 0.f);   // STEP: this thread's maxima over its tiles
 
     for (int tile = blockIdx.x; tile < args.ntiles; tile += gridDim.x) {
         const int q0 = tile * P;
@@ -491,7 +518,8 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
                 s[V::at(t, p)] = make_float2((float)(v.x * args.in_scale), (float)(v.y * args.in_scale));
             }
             __syncthreads();
-            nonlinear_tile<NT, P, true>(s, nullptr, args.nl, scan_mem, tid, args.tau_out, args.fe_out, q0, NP);
+            float4 unused = make_float4(0.f, 0.f, 0.f, 0.f);
+            nonlinear_tile<NT, P, true>(s, nullptr, args.nl, scan_mem, tid, args.tau_out, args.fe_out, q0, NP, unused);
             __syncthreads();
         } else if constexpr (MODE == PM_ENTRY_C128 || MODE == PM_ENTRY_C64) {
             // real-space input, reference layout A[t*NP + q]
@@ -580,7 +608,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             __syncthreads();
             dit_all<NT, NT, V>(s, tw, tid, TH);
 
-            nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP);
+            nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
             __syncthreads();
             dif_all<NT, NT, V>(s, tw, tid, TH);
             store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
@@ -590,6 +618,9 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
     if constexpr (MODE == PM_TEMP) {
         __syncthreads();
         for (int t = tid; t < NT; t += TH) atomicAdd(&args.temp[t], tsum[t]);
+    }
+    if constexpr (MODE == PM_STEP) {
+        if (args.stats) stats_max<TH>(mx, args.stats, reinterpret_cast<float*>(scan_mem), tid);
     }
 }
 

@@ -185,7 +185,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             s[V::at(t, p)] = mpc::cscale(A[(size_t)t * NP + q0 + p], in_scale);
         }
         __syncthreads();
-        mpc::nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP);
+        float4 mx = make_float4(0.f, 0.f, 0.f, 0.f);
+        mpc::nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
         __syncthreads();
         for (int f = tid; f < NT * P; f += kThreads) {
             const int t = f / P, p = f - t * P;
