@@ -491,17 +491,24 @@ static int split_tables(mpc_ctx* c, const TableSet& t) {
     return MPC_OK;
 }
 
+// Adaptive runs meet a new step length every few steps: once the cache holds more than 64
+// table sets, free them all.  Called at the start of an operation, before its first
+// get_tables, and never while launches are being captured: the sets an operation looks up stay
+// valid until its launches are queued, and the stream synchronisation here retires every launch
+// that used a freed set.
+static void recycle_tables(mpc_ctx* c) {
+    if (c->tables.size() <= 64 || c->capturing) return;
+    cudaStreamSynchronize(c->st);
+    for (auto& kv : c->tables) cudaFree(kv.second.f64);
+    c->tables.clear();
+}
+
 static int get_tables(mpc_ctx* c, double zd, double zp, double scale, TableSet* out) {
     auto key = std::make_tuple(zd, zp, scale);
     auto it = c->tables.find(key);
     if (it != c->tables.end()) {
         *out = it->second;
         return MPC_OK;
-    }
-    if (c->tables.size() > 64 && !c->capturing) {  // adaptive runs: recycle the cache
-        cudaStreamSynchronize(c->st);
-        for (auto& kv : c->tables) cudaFree(kv.second.f64);
-        c->tables.clear();
     }
     TableSet t;
     int rc = alloc_tables(c, &t);
@@ -926,6 +933,7 @@ int mpc_run_fixed(mpc_ctx* c, int nsteps) {
     auto bounce_after = [&](long g) -> int { return bounces_between((double)g * dz, (double)(g + 1) * dz, Cav); };
     int rc;
     TableSet t1, t2;
+    recycle_tables(c);
     // first half step of step g0 on the normalised state
     int s_prev = sign_of(g0);
     if ((rc = get_tables(c, s_prev * dz / 2, dz / 2, sNP, &t1))) return rc;
@@ -977,6 +985,7 @@ int mpc_ssfmprop(mpc_ctx* c, double* A, int sst_on, double dzz, int* signmem, do
     if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
     const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
     TableSet t1, t2;
+    recycle_tables(c);
     if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sNP, &t1))) return rc;
     if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sN, &t2))) return rc;
     if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;
@@ -1096,6 +1105,7 @@ int mpc_calcexpR(mpc_ctx* c, double* expR, int* signmem, double z, double dzz) {
     if (-*signmem == signum) *signmem = -*signmem;
     if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
     TableSet t;
+    recycle_tables(c);
     int rc = get_tables(c, signum * dzz, 0.0, 1.0, &t);
     if (rc) return rc;
     std::vector<double2> h(c->Nx);
@@ -1253,6 +1263,7 @@ static int step_double_launch(mpc_ctx* c) {
     if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
     const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
     int rc;
+    recycle_tables(c);
     // C1: one step of 2 dz
     TableSet a1, a2;
     if ((rc = get_tables(c, signum * dz, dz, sNP, &a1))) return rc;
@@ -1372,7 +1383,10 @@ int mpc_batch_destroy(mpc_batch* b) {
 // Capture per_cell(cell) for every active cell into one graph and run it to completion.
 static int batch_graph(mpc_batch* b, const std::vector<char>& active, const std::function<int(mpc_ctx*)>& per_cell) {
     for (size_t i = 0; i < b->cells.size(); i++)
-        if (active[i]) CK(cudaStreamSynchronize(b->cells[i]->st), "batch: cell stream");
+        if (active[i]) {
+            CK(cudaStreamSynchronize(b->cells[i]->st), "batch: cell stream");
+            recycle_tables(b->cells[i]);
+        }
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeRelaxed), "begin graph capture");
     int rc = MPC_OK;
     cudaError_t e = cudaEventRecord(b->fork, b->st);
@@ -1456,6 +1470,7 @@ int mpc_step(mpc_ctx* c, double dzz) {
     const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
     TableSet t1, t2;
     int rc;
+    recycle_tables(c);
     if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sNP, &t1))) return rc;
     if ((rc = get_tables(c, signum * dzz / 2, dzz / 2, sN, &t2))) return rc;
     if ((rc = launch_plane(c, c->S, c->S, t1, nullptr))) return rc;

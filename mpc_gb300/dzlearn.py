@@ -111,10 +111,15 @@ def load(path: str = DEFAULT_MODEL):
     return mlp
 
 
+def _cell(cfg):
+    return cfg if isinstance(cfg, tuple) else inputs.make_cell(cfg)
+
+
 def run_plain(cfg, variant: int = -1, def_err: float | None = None):
-    """Plain step doubling to dist: (field, executed split steps, seconds)."""
+    """Plain step doubling to dist: (field, executed split steps, seconds).  cfg: a CellConfig
+    or its (params, field) from inputs.make_cell."""
     from .capi import Propagator
-    p, A = inputs.make_cell(cfg)
+    p, A = _cell(cfg)
     if def_err is not None:
         p = p.copy(def_err=def_err)
     with Propagator(p.copy(variant=variant)) as prop:
@@ -133,7 +138,7 @@ def run_plain(cfg, variant: int = -1, def_err: float | None = None):
 def run_learned(cfg, mlp, safety: float = 0.9, check_every: int = 8, fallback_len: int = 4, variant: int = -1):
     """The learned controller to dist: (field, statistics, seconds)."""
     from .capi import Propagator
-    p, A = inputs.make_cell(cfg)
+    p, A = _cell(cfg)
     with Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
         prop.sync()
@@ -150,7 +155,7 @@ def run_reference(cfg, steps_per_pass: int, variant: int = -1):
     tolerance near the ~1e-7 rounding floor of its complex64 error estimate cannot serve: it
     shrinks dz to dzmin.)"""
     from .capi import Propagator
-    p, A = inputs.make_cell(cfg)
+    p, A = _cell(cfg)
     p = p.copy(dzz=p.Cav / steps_per_pass)
     with Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
@@ -164,6 +169,7 @@ def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, **kw) -> list[dict
     wall time of plain step doubling and of the learned controller."""
     rows = []
     for cfg in cfgs:
+        cfg = _cell(cfg)
         ref, n_ref = run_reference(cfg, ref_steps_per_pass)
         plain, n_plain, t_plain = run_plain(cfg)
         learned, st, t_learned = run_learned(cfg, mlp, **kw)

@@ -285,3 +285,24 @@ def test_mirror_bounce_lens(gpu_lib):
         got = prop.download()
         assert prop.state().puls_e == pytest.approx(p.puls_e * 0.95, rel=1e-12)
     assert rel(got, ref) < 1e-5
+
+
+def test_step_of_many_lengths_matches_oracle(gpu_lib):
+    """mpc_step with 120 different lengths (the phase-table cache is recycled on the way) follows
+    the oracle's split steps of the same lengths."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(Nx=16, Ny=16, Nt=64, window_xy=2e-3, window_t=1e-12, energy=0.3e-3)
+    lengths = p.dzz * 0.2 * (1.0 + 0.01 * np.arange(120))
+    assert lengths.sum() < p.Cav                       # no mirror plane on the way
+    ref = A.copy()
+    z, sm = 0.0, 1
+    for dz in lengths:
+        sm = o.ssfmprop(ref, float(dz), sm, z, p.puls_e)["signmem"]
+        z += dz
+    with Propagator(p) as prop:
+        prop.upload(A)
+        for dz in lengths:
+            prop.step(float(dz))
+        got = prop.download()
+        assert prop.state().z == pytest.approx(z, rel=1e-12) and prop.state().nstep == len(lengths)
+    assert rel(got, ref) < 1e-4
