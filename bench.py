@@ -177,7 +177,7 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     from mpc_gb300 import capi
     cfg, p, A = make_workload()
-    prop = capi.Propagator(p.copy(variant=-1))   # the autotuner picks the kernel variant
+    prop = capi.Propagator(p.copy(variant=args.variant))   # -1: the autotuner picks the kernel variant
     vinfo = prop.variant_info()
     # pinned host field for the end-to-end path (physical units, calibrated)
     pin = capi.PinnedArray(p.N)
@@ -269,13 +269,13 @@ def run_gb300(args):
         dist.barrier()
 
 
-def run_profile_case(nsteps: int):
+def run_profile_case(nsteps: int, variant: int = 0):
     """A short target for ncu: upload the workload's field and run `nsteps` split steps,
     with no timing.  Launch order: the entry pencil sweep (template mode 0), then per split
     step one pencil sweep (mode 2) and one plane sweep."""
     from mpc_gb300 import capi
     cfg, p, A = make_workload()
-    with capi.Propagator(p) as prop:
+    with capi.Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
         prop.run_fixed(nsteps)
         prop.sync()
@@ -289,11 +289,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="kernel variant of the grid (-1: autotune; pin one for profiler runs, whose "
+                         "serialised timings mislead the autotuner)")
     ap.add_argument("--profile-case", type=int, default=0, metavar="NSTEPS",
                     help="run NSTEPS split steps of the workload and exit (an ncu target)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case)
+        run_profile_case(args.profile_case, max(args.variant, 0))
     elif args.impl == "reference":
         run_reference(args)
     else:

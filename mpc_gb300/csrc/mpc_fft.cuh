@@ -212,8 +212,10 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, int n
     }
 }
 
-// DIT stage (exact transpose of the DIF stage with conjugate twiddles).
-template <int N, int L, class V>
+// DIT stage (exact transpose of the DIF stage with conjugate twiddles).  CORR = false skips the
+// (1 - eps) magnitude correction, for transforms whose result is not fed back into the field
+// (the time derivative of the self-steepening term).
+template <int N, int L, class V, bool CORR = true>
 __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
@@ -233,8 +235,12 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, int n
 #pragma unroll
             for (int k = 1; k < R; k++) {
                 const float2 u = cmulc(v[k], t[j * (k - 1) * (N / L)]);
-                const float e = te[j * (k - 1) * (N / L)];
-                v[k] = make_float2(fmaf(u.x, e, u.x), fmaf(u.y, e, u.y));
+                if constexpr (CORR) {
+                    const float e = te[j * (k - 1) * (N / L)];
+                    v[k] = make_float2(fmaf(u.x, e, u.x), fmaf(u.y, e, u.y));
+                } else {
+                    v[k] = u;
+                }
             }
         }
         dft<R, true>(v);
@@ -253,11 +259,11 @@ __device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid, int nth
 }
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
-template <int N, int L, class V>
+template <int N, int L, class V, bool CORR = true>
 __device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, int nthr) {
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dit_all<N, L / R, V>(s, tw, tid, nthr);
-    dit_stage<N, L, V>(s, tw, tid, nthr);
+    if constexpr (L / R > 1) dit_all<N, L / R, V, CORR>(s, tw, tid, nthr);
+    dit_stage<N, L, V, CORR>(s, tw, tid, nthr);
     __syncthreads();
 }
 

@@ -312,7 +312,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         }
         // S3: apply the nonlinear step (or emit the ionization outputs)
         float R = Rin;
-#pragma unroll 4
+#pragma unroll 2
         for (int i = 0; i < 32; i++) {
             const int t = t0 + i;
             const float2 a = w[V::walk(i)];
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             if (c.sst_c != 0.0f) {
                 load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
                 __syncthreads();
-                dit_all<NT, NT, V>(s, tw, tid, TH);
+                dit_all<NT, NT, V, false>(s, tw, tid, TH);
                 for (int f = tid; f < NT * P; f += TH) {
                     const int t = f / P, p = f - (f / P) * P;
                     scr[f] = s[V::at(t, p)];
