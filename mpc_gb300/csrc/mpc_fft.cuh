@@ -187,13 +187,16 @@ struct Twiddles {
 __host__ __device__ constexpr int twiddle_bytes(int N) { return N * 12; }
 
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
-template <int N, int L, class V>
-__device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, int nthr) {
+// NTH threads share the stage's TOT butterflies; UNR of a thread's butterflies are unrolled
+// together so that their shared-memory loads overlap.
+template <int N, int L, class V, int NTH, int UNR>
+__device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
     constexpr int TOT = NB * V::NLINES;
-    for (int idx = tid; idx < TOT; idx += nthr) {
+#pragma unroll UNR
+    for (int idx = tid; idx < TOT; idx += NTH) {
         const int line = idx % V::NLINES;
         const int g = idx / V::NLINES;
         const int b = g / S, j = g - (g / S) * S;
@@ -215,13 +218,14 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, int n
 // DIT stage (exact transpose of the DIF stage with conjugate twiddles).  CORR = false skips the
 // (1 - eps) magnitude correction, for transforms whose result is not fed back into the field
 // (the time derivative of the self-steepening term).
-template <int N, int L, class V, bool CORR = true>
-__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, int nthr) {
+template <int N, int L, class V, int NTH, int UNR, bool CORR = true>
+__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
     constexpr int TOT = NB * V::NLINES;
-    for (int idx = tid; idx < TOT; idx += nthr) {
+#pragma unroll UNR
+    for (int idx = tid; idx < TOT; idx += NTH) {
         const int line = idx % V::NLINES;
         const int g = idx / V::NLINES;
         const int b = g / S, j = g - (g / S) * S;
@@ -250,20 +254,20 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, int n
 }
 
 // Whole forward transform (natural -> position order).  Ends with a __syncthreads.
-template <int N, int L, class V>
-__device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid, int nthr) {
-    dif_stage<N, L, V>(s, tw, tid, nthr);
+template <int N, int L, class V, int NTH, int UNR = 1>
+__device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid) {
+    dif_stage<N, L, V, NTH, UNR>(s, tw, tid);
     __syncthreads();
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dif_all<N, L / R, V>(s, tw, tid, nthr);
+    if constexpr (L / R > 1) dif_all<N, L / R, V, NTH, UNR>(s, tw, tid);
 }
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
-template <int N, int L, class V, bool CORR = true>
-__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, int nthr) {
+template <int N, int L, class V, int NTH, int UNR = 1, bool CORR = true>
+__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid) {
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dit_all<N, L / R, V, CORR>(s, tw, tid, nthr);
-    dit_stage<N, L, V, CORR>(s, tw, tid, nthr);
+    if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR>(s, tw, tid);
+    dit_stage<N, L, V, NTH, UNR, CORR>(s, tw, tid);
     __syncthreads();
 }
 

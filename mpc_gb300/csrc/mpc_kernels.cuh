@@ -33,6 +33,12 @@ constexpr int kThreads = 512;          // threads of a one-CTA-per-SM launch (12
 #endif
 constexpr bool kPrefetch = MPC_PREFETCH != 0;
 constexpr int kTilePoints = 16384;     // default pencil tile: P * Nt complex points (128 KB)
+// butterflies of a pencil thread unrolled together per FFT stage (the plane sweep keeps 1: its
+// kernels are at the register limit)
+#ifndef MPC_PENCIL_UNROLL
+#define MPC_PENCIL_UNROLL 4
+#endif
+constexpr int kPencilUnroll = MPC_PENCIL_UNROLL;
 
 // FP32 constants of the nonlinear step, computed on the host in FP64.
 struct NLConst {
@@ -536,13 +542,13 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
                 s[V::at(t, p)] = e;
             }
             __syncthreads();
-            dif_all<NT, NT, V>(s, tw, tid, TH);
+            dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         } else if constexpr (MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP) {
             load_tile<NT, P, SLO, false>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
             __syncthreads();
-            dit_all<NT, NT, V>(s, tw, tid, TH);
+            dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             if constexpr (MODE == PM_TEMP) {
                 const double inv = args.out_scale * args.out_scale;
                 for (int t = tid; t < NT; t += TH) {
@@ -596,7 +602,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             if (c.sst_c != 0.0f) {
                 load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
                 __syncthreads();
-                dit_all<NT, NT, V, false>(s, tw, tid, TH);
+                dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid);
                 for (int f = tid; f < NT * P; f += TH) {
                     const int t = f / P, p = f - (f / P) * P;
                     scr[f] = s[V::at(t, p)];
@@ -606,11 +612,11 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             // A = IFFT_t(S)
             load_tile<NT, P, SLO, false>(s, gin, args.wpos, q0, NP, tid);
             __syncthreads();
-            dit_all<NT, NT, V>(s, tw, tid, TH);
+            dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
 
             nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
             __syncthreads();
-            dif_all<NT, NT, V>(s, tw, tid, TH);
+            dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         }
@@ -726,9 +732,9 @@ __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, cons
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
     using CV = ColView<NX, NY, CL, PB, SLO>;
-    dif_all<NX, NX, RV>(s, twx, tid, NTHR);
+    dif_all<NX, NX, RV, NTHR>(s, twx, tid);
     cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
-    dif_all<NY, NY, CV>(s, twy, tid, NTHR);
+    dif_all<NY, NY, CV, NTHR>(s, twy, tid);
     // multiply by Rx(px) and Ry(py) D(slot) (double-float factors)
     for (int e = tid; e < PB * NY * C::CX; e += NTHR) {
         const int xl = e % C::CX;
@@ -740,9 +746,9 @@ __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, cons
         s[idx] = cmul_df(cmul_df(s[idx], __ldg(&T.Rx[px])), __ldg(&T.RyD[(size_t)y * a.Nt + slot]));
     }
     __syncthreads();
-    dit_all<NY, NY, CV>(s, twy, tid, NTHR);
+    dit_all<NY, NY, CV, NTHR>(s, twy, tid);
     cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
-    dit_all<NX, NX, RV>(s, twx, tid, NTHR);
+    dit_all<NX, NX, RV, NTHR>(s, twx, tid);
 }
 
 // NTHR threads per CTA; 512 / NTHR CTAs per SM (the register file holds 512 threads at

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 s[V::at(t, p)] = mpc::cscale(A[(size_t)t * NP + q0 + p], in_scale);
             }
             __syncthreads();
-            mpc::dif_all<NT, NT, V>(s, tw, tid, kThreads);
+            mpc::dif_all<NT, NT, V, kThreads>(s, tw, tid);
             const float inv_nt = 1.0f / (float)NT;
             for (int f = tid; f < NT * P; f += kThreads) {
                 const int pos = f / P, p = f - pos * P;
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 s[i] = mpc::cscale(mpc::mul_mi<false>(s[i]), wpos[pos] * inv_nt);
             }
             __syncthreads();
-            mpc::dit_all<NT, NT, V>(s, tw, tid, kThreads);
+            mpc::dit_all<NT, NT, V, kThreads>(s, tw, tid);
             for (int f = tid; f < NT * P; f += kThreads) {
                 const int t = f / P, p = f - t * P;
                 scr[f] = s[V::at(t, p)];
