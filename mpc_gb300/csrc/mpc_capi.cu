@@ -797,7 +797,7 @@ int mpc_variant_info(mpc_ctx* c, int* variant, int* info) {
     if (!c || !variant || !info) return fail(MPC_ERR_ARG, "null argument");
     *variant = c->variant;
     const int v[8] = {c->ops->P, c->ops->SLO, c->ops->CL, c->ops->PB, c->ops->PT, c->pencil_grid,
-                      c->plane_clusters, c->ops->P * c->Nt / 32};
+                      c->plane_clusters, c->ops->P * c->Nt / c->ops->CH};
     for (int i = 0; i < 8; i++) info[i] = v[i];
     return MPC_OK;
 }

@@ -62,8 +62,9 @@ struct NLConst {
 // Pencil tile view: line = pencil p, element (pos, p).  For P < 16 a pad of P slots every
 // 2^SH positions and every 32 positions keeps the FFT stages and the per-thread t walks free
 // of shared-memory bank conflicts (SH = 4 for P = 8, 3 for P = 4).  The pad depends on pos
-// only through pos >> 3, >> 4 and >> 5, so a walk of 32 samples from a multiple of 32 has the
-// same offsets everywhere: at(t0 + i, p) - at(t0, p) == walk(i).
+// only through pos >> SH and pos >> 5, so a walk of CH samples from a multiple of CH has the
+// same offsets everywhere, at(t0 + i, p) - at(t0, p) == walk(i), for CH = 32 and, when SH = 4,
+// for CH = 16.
 template <int NT, int P>
 struct PencilView {
     static constexpr int NLINES = P;
@@ -115,7 +116,7 @@ __device__ __forceinline__ size_t slot_index(int s, int q, int NP, int SLO) {
 //   (u, v)_{k+1} = (u_k + c2_k v_k, g_k - u_k)     map (M, o): x -> M x + o
 // with a_k = W1 Kon, b_k = Wava Kon, c2_k = W2 Kon, g_k = 1 - exp(-R_k); u = ions2,
 // v = ions1, both zero before the first slice; fe_sp[k] = (v_k + 2 u_k) sigma_k.
-// Chunk maps are composed in FP32 inside a thread's 32 points and across chunks in FP64.
+// Chunk maps are composed in FP32 inside a thread's CH points and across chunks in FP64.
 // ---------------------------------------------------------------------------------------
 struct MapR { double B, C; };
 struct MapUV { double m00, m01, m10, m11, o0, o1; };
@@ -158,7 +159,7 @@ __device__ __forceinline__ M shfl_up_map(const M& m, int off) {
 template <class M, int P, int TPP>
 __device__ __forceinline__ void scan_chunks(M* maps, int tid) {
     const int warp = tid >> 5, lane = tid & 31;
-    constexpr int NW = P * TPP / 32;       // the CTA has one thread per 32-sample chunk
+    constexpr int NW = P * TPP / 32;       // the CTA has one thread per chunk
     constexpr int CPL = (TPP + 31) / 32;
     for (int p = warp; p < P; p += NW) {
         M* row = maps + p * TPP;
@@ -255,18 +256,19 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
 // IONIZ_ONLY = false: A *= exp(dz * A_nl) in place (propagation.c:244-327 with the A13/A14
 // fixes).  IONIZ_ONLY = true: write tau_c and freeelectrons_sp (plasma.c:118-245 outputs)
 // in the reference layout instead, A untouched.  Thread (p = tid % P, ch = tid / P) walks
-// the 32 samples t = 32 ch .. 32 ch + 31 of pencil p.  The step's running maxima go to `mx`:
+// the CH samples t = CH ch .. CH ch + CH - 1 of pencil p.  The step's running maxima go to `mx`:
 // {|a|^2 (device units), ionization fraction, |Im A_nl| (phase rate, rad/m), |Re A_nl| (1/m)}.
-template <int NT, int P, bool IONIZ_ONLY>
+template <int NT, int P, bool IONIZ_ONLY, int CH = 32>
 __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restrict__ scr, const NLConst& c,
                                                void* scan_mem, int tid, double* tau_out, double* fe_out,
                                                int q0, int NP, float4& mx) {
     using V = PencilView<NT, P>;
-    constexpr int TPP = NT / 32;
+    static_assert(CH == 32 || (CH == 16 && V::SH == 4), "walk offsets need a chunk-aligned pad");
+    constexpr int TPP = NT / CH;
     const int p = tid % P;
     const int ch = tid / P;
-    const int t0 = ch * 32;
-    float2* w = s + V::at(t0, p);   // this thread's 32 samples: w[V::walk(i)]
+    const int t0 = ch * CH;
+    float2* w = s + V::at(t0, p);   // this thread's CH samples: w[V::walk(i)]
     const float2* dA = scr + t0 * P + p;   // dA of the same samples: dA[i * P]
     if (c.plasma) {
         MapR* mr = reinterpret_cast<MapR*>(scan_mem);
@@ -276,7 +278,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         {
             float B = 0.0f, C = 0.0f;
 #pragma unroll 8
-            for (int i = 0; i < 32; i++) {
+            for (int i = 0; i < CH; i++) {
                 const IonPoint ip = ion_point(w[V::walk(i)], c);
                 const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
                 C = fmaf(1.0f - ip.b, C, Ck);
@@ -296,7 +298,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float R = Rin;
             float m00 = 1.f, m01 = 0.f, m10 = 0.f, m11 = 1.f, o0 = 0.f, o1 = 0.f;
 #pragma unroll 4
-            for (int i = 0; i < 32; i++) {
+            for (int i = 0; i < CH; i++) {
                 const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
                 R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
                 const float g = one_minus_exp_neg(R);
@@ -319,7 +321,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         // S3: apply the nonlinear step (or emit the ionization outputs)
         float R = Rin;
 #pragma unroll 2
-        for (int i = 0; i < 32; i++) {
+        for (int i = 0; i < CH; i++) {
             const int t = t0 + i;
             const float2 a = w[V::walk(i)];
             const IonPoint ip = ion_point(a, c);
@@ -352,7 +354,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         }
     } else {
 #pragma unroll 4
-        for (int i = 0; i < 32; i++) {
+        for (int i = 0; i < CH; i++) {
             const float2 a = w[V::walk(i)];
             const float a2 = fmaf(a.x, a.x, a.y * a.y);
             float re = 0.0f;
@@ -395,18 +397,21 @@ __device__ __forceinline__ void stats_max(float4 v, unsigned int* stats, float* 
 // Pencil pass
 // ---------------------------------------------------------------------------------------
 // Shared memory of a pencil CTA: [field tile][scan maps][W_Nt twiddles][FP64 t sums (TEMP)].
-// One thread per 32-sample chunk: TH = P * Nt / 32 threads.
-template <int NT, int P, int SLO>
+// One thread per CH-sample chunk of the nonlinear walk: TH = P * Nt / CH threads (CH = 16 puts
+// 1024 threads, 64 registers each, in a CTA: twice the warps to hide latency).
+template <int NT, int P, int SLO, int CH = 32>
 struct PencilCfg {
     using View = PencilView<NT, P>;
-    static constexpr int TPP = NT / 32;                 // 32-point chunks per pencil
+    static constexpr int TPP = NT / CH;                 // chunks per pencil
     static constexpr int TH = P * TPP;                  // threads per CTA
     static constexpr int SMEM_FIELD = View::SIZE * 8;  // bytes
     static constexpr int SMEM_SCAN = P * TPP * (int)sizeof(MapUV);
     static constexpr int SMEM_TW = twiddle_bytes(NT);
     static constexpr int SMEM_TEMP = NT * 8;            // FP64 temporal sums (TEMP mode only)
     static constexpr int SMEM = SMEM_FIELD + SMEM_SCAN + SMEM_TW;
-    static constexpr int SMEM_TEMP_MODE = SMEM + SMEM_TEMP;
+    // the TEMP mode keeps its sums in the scan area (unused there) when they fit
+    static constexpr bool TEMP_IN_SCAN = SMEM_SCAN >= SMEM_TEMP;
+    static constexpr int SMEM_TEMP_MODE = TEMP_IN_SCAN ? SMEM : SMEM + SMEM_TEMP;
     static constexpr int smem(int mode) { return mode == 5 ? SMEM_TEMP_MODE : SMEM; }
     static_assert(TH % 32 == 0 && TH <= 1024, "pencil CTA size");
     static_assert((P * SLO) % 2 == 0, "rows must be whole float4s");
@@ -414,11 +419,11 @@ struct PencilCfg {
 
 // L2 prefetch of the P*SLO*8 = 128 B rows of a slot-layout tile (overlaps the next tile's
 // DRAM reads with this tile's compute; one bulk prefetch per row)
-template <int NT, int P, int SLO>
+template <int NT, int P, int SLO, int TH>
 __device__ __forceinline__ void prefetch_tile(const float2* g, int q0, int NP, int tid) {
     constexpr int ROWS = NT / SLO;
     constexpr int BYTES = P * SLO * 8;
-    for (int row = tid; row < ROWS; row += PencilCfg<NT, P, SLO>::TH) {
+    for (int row = tid; row < ROWS; row += TH) {
         const float2* a = g + ((size_t)row * NP + q0) * SLO;
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "n"(BYTES) : "memory");
     }
@@ -428,14 +433,14 @@ __device__ __forceinline__ void prefetch_tile(const float2* g, int q0, int NP, i
 // (pos 2r, pos 2r + 1) of one pencil; odd rows store them in the opposite order so that
 // the four rows a warp touches fall on both halves of the shared-memory banks.
 // load a slot-layout tile into shared memory, optionally multiplied by -i*omega(pos)
-template <int NT, int P, int SLO, bool DERIV>
+template <int NT, int P, int SLO, bool DERIV, int TH>
 __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ g, const float* __restrict__ wpos,
                                           int q0, int NP, int tid) {
     using V = PencilView<NT, P>;
     constexpr int F4_PER_ROW = P * SLO / 2;
     constexpr int ROWS = NT / SLO;
     const float4* g4 = reinterpret_cast<const float4*>(g);
-    for (int f = tid; f < ROWS * F4_PER_ROW; f += PencilCfg<NT, P, SLO>::TH) {
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += TH) {
         const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
         const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
         const float4 v = __ldg(&g4[gi]);
@@ -458,13 +463,13 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
     }
 }
 
-template <int NT, int P, int SLO>
+template <int NT, int P, int SLO, int TH>
 __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__ g, int q0, int NP, int tid) {
     using V = PencilView<NT, P>;
     constexpr int F4_PER_ROW = P * SLO / 2;
     constexpr int ROWS = NT / SLO;
     float4* g4 = reinterpret_cast<float4*>(g);
-    for (int f = tid; f < ROWS * F4_PER_ROW; f += PencilCfg<NT, P, SLO>::TH) {
+    for (int f = tid; f < ROWS * F4_PER_ROW; f += TH) {
         const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
         const size_t gi = (((size_t)row * NP + q0) * SLO) / 2 + c;
         int pos0, p0, pos1, p1;
@@ -482,17 +487,17 @@ __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__
     }
 }
 
-template <int NT, int P, int SLO, int MODE>
-__global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, SLO>::TH >= kThreads ? 1 : 2))
+template <int NT, int P, int SLO, int MODE, int CH = 32>
+__global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, P, SLO, CH>::TH >= kThreads ? 1 : 2))
     pencil_kernel(PencilArgs args) {
-    using Cfg = PencilCfg<NT, P, SLO>;
+    using Cfg = PencilCfg<NT, P, SLO, CH>;
     using V = typename Cfg::View;
     constexpr int TH = Cfg::TH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
     void* scan_mem = smem_raw + Cfg::SMEM_FIELD;
     unsigned char* tw_mem = smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN;
-    double* tsum = reinterpret_cast<double*>(smem_raw + Cfg::SMEM);
+    double* tsum = reinterpret_cast<double*>(Cfg::TEMP_IN_SCAN ? smem_raw + Cfg::SMEM_FIELD : smem_raw + Cfg::SMEM);
     const int tid = threadIdx.x;
     const int NP = args.NP;
     {
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
         if constexpr (kPrefetch && (MODE == PM_STEP || MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP)) {
             const int nxt = tile + gridDim.x;
             if (nxt < args.ntiles)
-                prefetch_tile<NT, P, SLO>(reinterpret_cast<const float2*>(args.in), nxt * P, NP, tid);
+                prefetch_tile<NT, P, SLO, TH>(reinterpret_cast<const float2*>(args.in), nxt * P, NP, tid);
         }
         if constexpr (MODE == PM_IONIZ) {
             for (int f = tid; f < NT * P; f += TH) {
@@ -525,7 +530,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             }
             __syncthreads();
             float4 unused = make_float4(0.f, 0.f, 0.f, 0.f);
-            nonlinear_tile<NT, P, true>(s, nullptr, args.nl, scan_mem, tid, args.tau_out, args.fe_out, q0, NP, unused);
+            nonlinear_tile<NT, P, true, CH>(s, nullptr, args.nl, scan_mem, tid, args.tau_out, args.fe_out, q0, NP, unused);
             __syncthreads();
         } else if constexpr (MODE == PM_ENTRY_C128 || MODE == PM_ENTRY_C64) {
             // real-space input, reference layout A[t*NP + q]
@@ -543,10 +548,10 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             }
             __syncthreads();
             dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
-            store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
+            store_tile<NT, P, SLO, TH>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         } else if constexpr (MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP) {
-            load_tile<NT, P, SLO, false>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
+            load_tile<NT, P, SLO, false, TH>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
             __syncthreads();
             dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             if constexpr (MODE == PM_TEMP) {
@@ -600,7 +605,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
             // dA = IFFT_t(-i omega S): the time derivative of the self-steepening term, kept in
             // this CTA's scratch tile [t][p] (L2-resident) until the nonlinear walk
             if (c.sst_c != 0.0f) {
-                load_tile<NT, P, SLO, true>(s, gin, args.wpos, q0, NP, tid);
+                load_tile<NT, P, SLO, true, TH>(s, gin, args.wpos, q0, NP, tid);
                 __syncthreads();
                 dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid);
                 for (int f = tid; f < NT * P; f += TH) {
@@ -610,14 +615,14 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO>::TH, (PencilCfg<NT, P, S
                 __syncthreads();
             }
             // A = IFFT_t(S)
-            load_tile<NT, P, SLO, false>(s, gin, args.wpos, q0, NP, tid);
+            load_tile<NT, P, SLO, false, TH>(s, gin, args.wpos, q0, NP, tid);
             __syncthreads();
             dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
 
-            nonlinear_tile<NT, P, false>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
+            nonlinear_tile<NT, P, false, CH>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
             __syncthreads();
             dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
-            store_tile<NT, P, SLO>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
+            store_tile<NT, P, SLO, TH>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         }
     }

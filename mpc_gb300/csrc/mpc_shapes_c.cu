@@ -1,4 +1,4 @@
-// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt), four layout / launch
+// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt), five layout / launch
 // variants (all give identical results; variant 0 is the default, the autotuner times all).
 #include "mpc_shapes.cuh"
 
@@ -9,5 +9,6 @@ const ShapeOps* const shape_list_c[] = {
     Shape<256,256,2048>::ops(),            // SLO 2, plane 512 threads, clusters of 8 (2 planes)
     Shape<256,256,2048,1,512>::ops(),      // SLO 1, plane 512 threads, clusters of 4
     Shape<256,256,2048,1,256,8192>::ops(), // SLO 1, 4-pencil tiles, 256-thread pencil and plane CTAs
+    Shape<256,256,2048,1,256,16384,16>::ops(),  // SLO 1, 1024-thread pencil CTAs (16-sample chunks)
     nullptr};
 }  // namespace mpc

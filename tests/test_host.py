@@ -124,14 +124,14 @@ def test_position_frequency_table(N):
 
 
 def _compiled_variants():
-    """(Nx, Ny, Nt, SLO, PT, TP) of every Shape<...>::ops() entry of the shape lists."""
+    """(Nx, Ny, Nt, SLO, PT, TP, CH) of every Shape<...>::ops() entry of the shape lists."""
     import glob
     import re
     out = []
     for f in sorted(glob.glob(os.path.join(ROOT, "mpc_gb300", "csrc", "mpc_shapes_*.cu"))):
         for m in re.finditer(r"Shape<([\d,\s]+)>::ops\(\)", open(f).read()):
             v = [int(x) for x in m.group(1).split(",")]
-            v += [0, 512, 16384][len(v) - 3:]
+            v += [0, 512, 16384, 32][len(v) - 3:]
             out.append(tuple(v))
     return out
 
@@ -139,7 +139,7 @@ def _compiled_variants():
 SHAPES = _compiled_variants()
 
 
-def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384):
+def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32):
     """Tile and cluster parameters, as mpc_shapes.cuh derives them."""
     P = TP // NT
     SLO = SLO_ if SLO_ > 0 else (16 // P if P < 16 else 1)
@@ -179,7 +179,7 @@ def _views(*variant):
 
 
 def test_variant_list_parsed():
-    assert (256, 256, 2048, 0, 512, 16384) in SHAPES
+    assert (256, 256, 2048, 0, 512, 16384, 32) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16) in SHAPES
     assert len({v[:3] for v in SHAPES}) >= 7
 
 
@@ -194,10 +194,11 @@ def _wavefronts(addrs):
 
 @pytest.mark.parametrize("shape", SHAPES)
 def test_pencil_view_bank_conflict_free(shape):
-    """Every FFT stage of the pencil tile and the 32-sample t walk of the nonlinear step take
+    """Every FFT stage of the pencil tile and the CH-sample t walk of the nonlinear step take
     the minimum two wavefronts per warp access (no bank conflicts)."""
     name, N, P, at, size = _views(*shape)[0]
-    nthr = N * P // 32
+    CH = shape[6]
+    nthr = N * P // CH
     L = N
     while L > 1:
         R = 16 if L >= 16 else L
@@ -210,8 +211,9 @@ def test_pencil_view_bank_conflict_free(shape):
                     addrs.append(at((g // S) * L + g % S + S * q, line))
                 assert _wavefronts(addrs) <= 2, (shape, L, w0, q)
         L //= R
-    for i in range(32):
-        assert _wavefronts([at(32 * (t // P) + i, t % P) for t in range(32)]) <= 2, (shape, i)
+    for w0 in range(0, min(nthr, 256), 32):
+        for i in range(CH):
+            assert _wavefronts([at(CH * (t // P) + i, t % P) for t in range(w0, w0 + 32)]) <= 2, (shape, i)
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -221,8 +223,9 @@ def test_fft_views_stage_separable_and_in_bounds(shape):
     is inside the view's shared-memory buffer, and that the view is one-to-one."""
     for name, N, NL, at, size in _views(*shape):
         if name == "pencil":   # the walk offsets of the nonlinear step equal at(t0 + i) - at(t0)
-            for t0 in range(0, N, 32):
-                for i in range(32):
+            CH = shape[6]
+            for t0 in range(0, N, CH):
+                for i in range(CH):
                     assert at(t0 + i, 0) - at(t0, 0) == at(i, 0) - at(0, 0), (t0, i)
         seen = set()
         for pos in range(N):
