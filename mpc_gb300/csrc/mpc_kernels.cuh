@@ -463,6 +463,38 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
     }
 }
 
+// Asynchronous tile load for the SLO = 1 layout: every 16 B chunk of a t-row (pencils 2c and
+// 2c + 1 at one position) is copied from global to shared memory by cp.async, all of them in
+// flight at once instead of each thread waiting on its loads in turn.  Both addresses are 16 B
+// aligned: NP and q0 are even, and P and the view's pad are even.  The caller waits with
+// cp_async_wait_all() and synchronises the CTA before using the tile.
+template <int NT, int P, int TH>
+__device__ __forceinline__ void load_tile_async(float2* s, const float2* __restrict__ g, int q0, int NP, int tid) {
+    using V = PencilView<NT, P>;
+    static_assert(P % 2 == 0, "16 B chunks of two pencils");
+    constexpr int F4_PER_ROW = P / 2;
+    const float4* g4 = reinterpret_cast<const float4*>(g);
+    for (int f = tid; f < NT * F4_PER_ROW; f += TH) {
+        const int row = f / F4_PER_ROW, c = f - row * F4_PER_ROW;
+        const float4* src = g4 + (((size_t)row * NP + q0) / 2 + c);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(s + V::at(row, 2 * c));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// In place: S(pos) -> -i omega(pos) S(pos), the spectrum of the time derivative.
+template <int NT, int P, int TH>
+__device__ __forceinline__ void times_minus_i_omega(float2* s, const float* __restrict__ wpos, int tid) {
+    using V = PencilView<NT, P>;
+    for (int e = tid; e < NT * P; e += TH) {
+        const int pos = e / P, p = e - (e / P) * P;
+        const int i = V::at(pos, p);
+        s[i] = cscale(mul_mi<false>(s[i]), __ldg(&wpos[pos]));
+    }
+}
+
 template <int NT, int P, int SLO, int TH>
 __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__ g, int q0, int NP, int tid) {
     using V = PencilView<NT, P>;
@@ -605,7 +637,14 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
             // dA = IFFT_t(-i omega S): the time derivative of the self-steepening term, kept in
             // this CTA's scratch tile [t][p] (L2-resident) until the nonlinear walk
             if (c.sst_c != 0.0f) {
-                load_tile<NT, P, SLO, true, TH>(s, gin, args.wpos, q0, NP, tid);
+                if constexpr (SLO == 1) {
+                    load_tile_async<NT, P, TH>(s, gin, q0, NP, tid);
+                    cp_async_wait_all();
+                    __syncthreads();
+                    times_minus_i_omega<NT, P, TH>(s, args.wpos, tid);
+                } else {
+                    load_tile<NT, P, SLO, true, TH>(s, gin, args.wpos, q0, NP, tid);
+                }
                 __syncthreads();
                 dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid);
                 for (int f = tid; f < NT * P; f += TH) {
@@ -615,7 +654,12 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
                 __syncthreads();
             }
             // A = IFFT_t(S)
-            load_tile<NT, P, SLO, false, TH>(s, gin, args.wpos, q0, NP, tid);
+            if constexpr (SLO == 1) {
+                load_tile_async<NT, P, TH>(s, gin, q0, NP, tid);
+                cp_async_wait_all();
+            } else {
+                load_tile<NT, P, SLO, false, TH>(s, gin, args.wpos, q0, NP, tid);
+            }
             __syncthreads();
             dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
 
