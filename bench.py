@@ -36,6 +36,14 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "grid-point-steps/s"
 STEPS_PER_PASS = 400
 BYTES_PER_PT_STEP = 32  # two compulsory complex64 sweeps (read + write) per split step
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 vector rate, nominal
+
+
+def fft_flop_per_pt_step(Nx: int, Ny: int, Nt: int) -> float:
+    """FFT work of one split step per grid point at 5 n log2(n) per transform: three Nt-point
+    t transforms (the self-steepening derivative, to time, back) and four x / y transforms."""
+    import math
+    return 3 * 5 * math.log2(Nt) + 2 * 5 * math.log2(Nx) + 2 * 5 * math.log2(Ny)
 
 
 def peaks():
@@ -252,6 +260,12 @@ def run_gb300(args):
         dt = cpu_baseline_run(p, A, nst, cores)
         cpu = {"value": p.N * nst / dt, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
                "sample": f"{nst} split steps of the 256x256x2048 cell, FP64 oracle/ restatement, OpenMP"}
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = nsm * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
+    fft_tflops = (value / world) * fft_flop_per_pt_step(p.Nx, p.Ny, p.Nt) / 1e12
+    fft_rate = {"flop_per_pt_step": fft_flop_per_pt_step(p.Nx, p.Ny, p.Nt), "tflops": fft_tflops,
+                "fp32_peak_tflops": fp32_peak, "frac_fp32": fft_tflops / fp32_peak,
+                "fp64_nominal_tflops": FP64_NOMINAL_TFLOPS, "ratio_to_fp64": fft_tflops / FP64_NOMINAL_TFLOPS}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -261,7 +275,8 @@ def run_gb300(args):
                                        "lens mirror, SST + ADK + plasma on", "grid": [p.Nx, p.Ny, p.Nt],
                            "split_steps_per_step": STEPS_PER_PASS, "l2": "field 1 GiB > L2, no flush",
                            "parallelism": f"replicas x{world}", "kernel_variant": vinfo},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+                "roofline": roofline, "fft_rate": fft_rate, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
     prop.close()
     pin.free()

@@ -306,3 +306,36 @@ def test_step_of_many_lengths_matches_oracle(gpu_lib):
         got = prop.download()
         assert prop.state().z == pytest.approx(z, rel=1e-12) and prop.state().nstep == len(lengths)
     assert rel(got, ref) < 1e-4
+
+
+def test_error_paths_return_status_and_leave_the_context_usable(gpu_lib):
+    """Errors come back as status codes with a message (the reference prints and exits or
+    carries on): unsupported grid, Nx != Ny, a variant past the last, calls before a field is
+    uploaded, null arguments, a non-positive step; afterwards the context still works."""
+    from mpc_gb300.capi import ERRORS, MPCError, Propagator
+    lib = gpu_lib
+    p, A, o = small_cell()
+    assert lib.mpc_shape_supported(48, 48, 300) == 0 and lib.mpc_shape_supported(p.Nx, p.Ny, p.Nt) == 1
+    for bad, code in ((p.copy(dims=(48, 48, 300), betas=np.zeros(300), w=np.zeros(300), wr=np.zeros(48),
+                                  r=np.zeros(48)), "MPC_ERR_SHAPE"),
+                      (p.copy(dims=(32, 16, 256), wr=np.zeros(16), r=np.zeros(16)), "MPC_ERR_SHAPE"),
+                      (p.copy(variant=99), "MPC_ERR_ARG"),
+                      (p.copy(variant=-2), "MPC_ERR_ARG")):
+        with pytest.raises(MPCError, match=code):
+            Propagator(bad)
+    with Propagator(p) as prop:
+        for call in (lambda: prop.run_fixed(3), lambda: prop.download(), lambda: prop.step_double(),
+                     lambda: prop.step(1e-3), lambda: prop.energy()):
+            with pytest.raises(MPCError, match="MPC_ERR_STATE"):
+                call()
+        assert lib.mpc_run_fixed(None, 1) == 1                       # MPC_ERR_ARG
+        assert lib.mpc_ssfmprop(prop.h, None, 1, 0.01, None, 0.0, None, None, None, None, None, None, None, 0) == 1
+        assert b"null" in lib.mpc_last_error()
+        prop.upload(A)
+        with pytest.raises(MPCError, match="MPC_ERR_ARG"):
+            prop.step(0.0)
+        with pytest.raises(MPCError, match="MPC_ERR_ARG"):
+            prop.mirror_bounce(7)
+        prop.run_fixed(2)                                            # still usable
+        assert prop.state().nstep == 2 and np.isfinite(prop.download()).all()
+    assert set(ERRORS.values()) >= {"MPC_ERR_ARG", "MPC_ERR_SHAPE", "MPC_ERR_STATE"}
