@@ -339,3 +339,24 @@ def test_error_paths_return_status_and_leave_the_context_usable(gpu_lib):
         prop.run_fixed(2)                                            # still usable
         assert prop.state().nstep == 2 and np.isfinite(prop.download()).all()
     assert set(ERRORS.values()) >= {"MPC_ERR_ARG", "MPC_ERR_SHAPE", "MPC_ERR_STATE"}
+
+
+@pytest.mark.parametrize("grid", [(128, 128, 1024), (256, 256, 512), (256, 256, 2048)])
+def test_production_grids_match_oracle(gpu_lib, grid):
+    """Two split steps on the sweep's and the benchmark's grids (autotuned kernel variant,
+    lens mirror, SST + ADK + plasma) against the FP64 oracle: the split-step tolerance."""
+    from mpc_gb300.capi import Propagator
+    Nx, Ny, Nt = grid
+    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048,
+                         energy=1e-3, bounce=BOUNCE_LENS)
+    p, A = inputs.make_cell(cfg)
+    o = oracle.Oracle(p)
+    o.calibrate(A)
+    ref = A.copy()
+    st = o.new_state()
+    o.run_fixed(ref, st, 2)
+    with Propagator(p.copy(variant=-1)) as prop:
+        prop.upload(A)
+        prop.run_fixed(2)
+        got = prop.download()
+    assert rel(got, ref) < 1e-5
