@@ -16,8 +16,26 @@
 
 namespace mpc {
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add and subtract as packed FP32x2 instructions (one instruction for both parts; each
+// part rounded exactly as the scalar operation): a - b is computed as fma(b, -1, a), whose
+// single rounding of the exact a - b equals the subtraction's.
+#ifndef MPC_PACKED_F32X2
+#define MPC_PACKED_F32X2 1
+#endif
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#if MPC_PACKED_F32X2
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#if MPC_PACKED_F32X2
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
