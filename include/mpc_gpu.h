@@ -56,6 +56,9 @@ typedef struct {
     int variant;            /* compiled kernel variant of this grid (layout and launch shapes; all
                                give the same results): 0 = default, k = the k-th, -1 = the
                                fastest, timed when the context is created */
+    int land_mirrors;       /* step doubling: 0 = as the reference, a bounce is applied after the
+                               attempt that crosses a mirror plane; 1 = an attempt that would cross
+                               the next plane is shortened to end on it */
 } mpc_params;
 
 typedef struct mpc_ctx mpc_ctx;

@@ -33,7 +33,7 @@ class c_mpc_params(C.Structure):
                 ("n0", C.c_double), ("puls_e", C.c_double), ("Ab_M", C.c_double), ("r", _dp),
                 ("dr", C.c_double), ("def_err", C.c_double), ("dzmin", C.c_double), ("Esig", C.c_double),
                 ("gas", C.c_char * 9), ("bounce_mode", C.c_int), ("roc", C.c_double),
-                ("variant", C.c_int)]
+                ("variant", C.c_int), ("land_mirrors", C.c_int)]
 
 
 class c_mpc_state(C.Structure):
@@ -162,6 +162,7 @@ class Propagator:
         cp.gas = p.gas.encode("ascii")[:8]
         cp.bounce_mode, cp.roc = p.bounce_mode, p.roc
         cp.variant = p.variant
+        cp.land_mirrors = p.land_mirrors
         self._cp = cp
         h = C.c_void_p()
         _check(self.lib.mpc_create(C.byref(h), C.byref(cp)), "mpc_create")

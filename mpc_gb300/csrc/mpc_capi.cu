@@ -308,6 +308,8 @@ struct mpc_ctx {
     unsigned int* dstats = nullptr;  // running maxima of the split steps since the last reset (4)
     double* dmom = nullptr;          // field moments (7 doubles) and max |S|^2 (bits, after them)
     double sd_dz = 0.0;      // dz of the attempt in flight
+    double sd_natural = 0.0; // the step before landing on a mirror plane shortened it
+    int sd_clipped = 0;      // the attempt in flight was shortened to land on a mirror plane
     int capturing = 0;       // launches are being captured into a CUDA graph (no synchronous calls)
     float* wpos = nullptr;
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
@@ -1255,7 +1257,17 @@ static int step_double_launch(mpc_ctx* c) {
         return fail(MPC_ERR_NOMEM, "cudaMallocHost step-doubling sums");
     }
     mpc_state& st = c->state;
-    const double dz = st.dzz, Cav = c->p.Cav;
+    const double Cav = c->p.Cav;
+    double dz = st.dzz;
+    c->sd_clipped = 0;
+    if (c->p.land_mirrors) {   // end the attempt on the next mirror plane rather than cross it
+        const double room = (floor(st.z / Cav + 1e-9) + 1.0) * Cav - st.z;
+        if (room > 1e-9 * Cav && 2.0 * dz > room) {
+            c->sd_natural = dz;
+            dz = room / 2.0;
+            c->sd_clipped = 1;
+        }
+    }
     c->sd_dz = dz;
     // calcexpR's sign logic (propagation.c:377-382), evaluated at the attempt's z for all three steps
     int signum = pass_sign(st.z, Cav);
@@ -1310,7 +1322,10 @@ static int step_double_finish(mpc_ctx* c, double* BP1, double* BP2, int* bad, do
     if (BP2) memcpy(BP2, h + 2 + c->Nx, sizeof(double) * c->Ny);
     *err = sqrt(h[0]) / sqrt(h[1]);
     st.err = *err;
+    if (c->sd_clipped) st.dzz = c->sd_dz;   // the rule judges the step taken
     step_rule(*err, &st.dzz, c->p.def_err, c->p.dzmin, st.y1, st.y2, bad);
+    // a shortening that only served to land on a plane does not shrink the next step
+    if (c->sd_clipped && !*bad && *err <= c->p.def_err && st.dzz < c->sd_natural) st.dzz = c->sd_natural;
     st.bad = *bad;
     st.attempts++;
     if (*bad) return MPC_OK;

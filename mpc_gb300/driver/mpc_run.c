@@ -2,7 +2,7 @@
  * mpc_run -- the run driver of the multipass-cell propagator, in place of the reference's
  * MPC.c (MPC.c:23-596), on libmpc_gpu.so through include/mpc_gpu.h.
  *
- *   mpc_run [-r] [-n NRUN] [-d DATADIR] [-m signflip|lens] [-R ROC] [-f CHUNK] [-v VARIANT]
+ *   mpc_run [-r] [-n NRUN] [-d DATADIR] [-m signflip|lens] [-R ROC] [-f CHUNK] [-v VARIANT] [-L]
  *
  * Files and formats are the reference's (MPC.c:77-110, 159-203, 489-509, 521-537, 558):
  *   DATADIR%04d/param.bin            run parameters, read field by field (MPC.c:180-203)
@@ -20,7 +20,8 @@
  * loop iteration of MPC.c:269-383).  -f CHUNK runs fixed steps of param.bin's dzz instead
  * (mpc_run_fixed, CHUNK steps between diagnostic records; other.bin then records err = 0).
  * -m lens -R ROC models each mirror as a focusing phase of radius of curvature ROC [m]
- * (param.bin carries no ROC); the default is the reference's diffraction sign flip.
+ * (param.bin carries no ROC); the default is the reference's diffraction sign flip.  -L ends
+ * step-doubling attempts on the mirror planes instead of stepping across them.
  *
  * Differences from MPC.c, all deliberate: the field is calibrated with both parts scaled
  * (MPC.c:213 scales the real part only) and only on a fresh run (the checkpointed field is
@@ -152,7 +153,7 @@ static void read_params(const char *dir, mpc_params *p, double **arrays) {
 static const char *kDiagFiles[5] = {"bp1.bin", "bp2.bin", "temp.bin", "spec.bin", "other.bin"};
 
 int main(int argc, char **argv) {
-    int resume = 0, nrun = 0, chunk = 0, variant = -1, bounce = MPC_BOUNCE_SIGNFLIP;
+    int resume = 0, nrun = 0, chunk = 0, variant = -1, bounce = MPC_BOUNCE_SIGNFLIP, land = 0;
     double roc = 0.0;
     const char *datadir = ".";
     for (int i = 1; i < argc; i++) {
@@ -163,6 +164,7 @@ int main(int argc, char **argv) {
         else if (!strcmp(a, "-d") && v) datadir = argv[++i];
         else if (!strcmp(a, "-f") && v) chunk = atoi(argv[++i]);
         else if (!strcmp(a, "-v") && v) variant = atoi(argv[++i]);
+        else if (!strcmp(a, "-L")) land = 1;
         else if (!strcmp(a, "-R") && v) roc = atof(argv[++i]);
         else if (!strcmp(a, "-m") && v) {
             const char *m = argv[++i];
@@ -170,7 +172,7 @@ int main(int argc, char **argv) {
             else if (!strcmp(m, "signflip")) bounce = MPC_BOUNCE_SIGNFLIP;
             else die("-m takes signflip or lens");
         } else {
-            fprintf(stderr, "usage: %s [-r] [-n NRUN] [-d DATADIR] [-m signflip|lens] [-R ROC] [-f CHUNK] [-v VARIANT]\n",
+            fprintf(stderr, "usage: %s [-r] [-n NRUN] [-d DATADIR] [-m signflip|lens] [-R ROC] [-f CHUNK] [-v VARIANT] [-L]\n",
                     argv[0]);
             return 2;
         }
@@ -186,6 +188,7 @@ int main(int argc, char **argv) {
     p.bounce_mode = bounce;
     p.roc = roc;
     p.variant = variant;
+    p.land_mirrors = land;
     const int Nx = p.dims[0], Ny = p.dims[1], Nt = p.dims[2];
     const size_t N = (size_t)Nx * Ny * Nt;
     printf("Matrix dimensions are: %d x %d x %d.\n", Nx, Ny, Nt);

@@ -115,13 +115,15 @@ def _cell(cfg):
     return cfg if isinstance(cfg, tuple) else inputs.make_cell(cfg)
 
 
-def run_plain(cfg, variant: int = -1, def_err: float | None = None):
+def run_plain(cfg, variant: int = -1, def_err: float | None = None, land: bool = False):
     """Plain step doubling to dist: (field, executed split steps, seconds).  cfg: a CellConfig
-    or its (params, field) from inputs.make_cell."""
+    or its (params, field) from inputs.make_cell; land: end attempts on the mirror planes (the
+    reference steps across them and applies the bounce after the attempt)."""
     from .capi import Propagator
     p, A = _cell(cfg)
     if def_err is not None:
         p = p.copy(def_err=def_err)
+    p = p.copy(land_mirrors=int(land))
     with Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
         prop.sync()
@@ -136,9 +138,11 @@ def run_plain(cfg, variant: int = -1, def_err: float | None = None):
 
 
 def run_learned(cfg, mlp, safety: float = 0.9, check_every: int = 8, fallback_len: int = 4, variant: int = -1):
-    """The learned controller to dist: (field, statistics, seconds)."""
+    """The learned controller to dist: (field, statistics, seconds).  Its own steps land on the
+    mirror planes, and so do its step-doubling checks and fallbacks."""
     from .capi import Propagator
     p, A = _cell(cfg)
+    p = p.copy(land_mirrors=1)
     with Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
         prop.sync()
@@ -164,22 +168,32 @@ def run_reference(cfg, steps_per_pass: int, variant: int = -1):
         return prop.download(), n
 
 
-def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, **kw) -> list[dict]:
+def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, safeties=(0.9,), **kw) -> list[dict]:
     """Per cell: end-field relative L2 error against a fine fixed-step run, executed steps and
-    wall time of plain step doubling and of the learned controller."""
+    wall time of plain step doubling (as the reference: bounces after the attempt that crosses a
+    mirror plane; and landing on the planes) and of the learned controller at each safety
+    factor.  The err_learned / steps_learned / seconds_learned keys are the first safety's."""
     rows = []
     for cfg in cfgs:
         cfg = _cell(cfg)
         ref, n_ref = run_reference(cfg, ref_steps_per_pass)
-        plain, n_plain, t_plain = run_plain(cfg)
-        learned, st, t_learned = run_learned(cfg, mlp, **kw)
         nr = np.linalg.norm(ref)
-        rows.append(dict(err_plain=float(np.linalg.norm(plain - ref) / nr),
-                         err_learned=float(np.linalg.norm(learned - ref) / nr),
-                         steps_plain=int(n_plain), steps_learned=int(st["executed_steps"]),
-                         seconds_plain=t_plain, seconds_learned=t_learned, speedup=t_plain / t_learned,
-                         checks=st["checks"], check_failures=st["check_failures"],
-                         fallback_attempts=st["fallback_attempts"], ref_steps=int(n_ref)))
+        plain, n_plain, t_plain = run_plain(cfg)
+        landed, n_landed, t_landed = run_plain(cfg, land=True)
+        row = dict(err_plain=float(np.linalg.norm(plain - ref) / nr), steps_plain=int(n_plain), seconds_plain=t_plain,
+                   err_plain_landing=float(np.linalg.norm(landed - ref) / nr), steps_plain_landing=int(n_landed),
+                   seconds_plain_landing=t_landed, ref_steps=int(n_ref), learned={})
+        for sf in safeties:
+            learned, st, t_learned = run_learned(cfg, mlp, safety=sf, **kw)
+            row["learned"][sf] = dict(err=float(np.linalg.norm(learned - ref) / nr), steps=int(st["executed_steps"]),
+                                      seconds=t_learned, checks=st["checks"], check_failures=st["check_failures"],
+                                      fallback_attempts=st["fallback_attempts"])
+        first = row["learned"][safeties[0]]
+        row.update(err_learned=first["err"], steps_learned=first["steps"], seconds_learned=first["seconds"],
+                   speedup=t_plain / first["seconds"], speedup_vs_landing=t_landed / first["seconds"],
+                   checks=first["checks"], check_failures=first["check_failures"],
+                   fallback_attempts=first["fallback_attempts"])
+        rows.append(row)
     return rows
 
 
@@ -203,7 +217,7 @@ def main(argv=None) -> int:
     e.add_argument("--seed", type=int, default=1000)
     e.add_argument("--grid", default="256,256,2048")
     e.add_argument("--passes", type=int, default=8)
-    e.add_argument("--safety", type=float, default=0.9)
+    e.add_argument("--safety", default="0.9", help="comma-separated safety factors of the learned controller")
     e.add_argument("--ref-steps", type=int, default=2000, help="fixed steps per pass of the reference run")
     a = ap.parse_args(argv)
     if a.cmd == "collect":
@@ -229,12 +243,17 @@ def main(argv=None) -> int:
     else:
         grid = tuple(int(v) for v in a.grid.split(","))
         cfgs = controller_cells(a.seed, a.cells, grid, passes=a.passes, steps_per_pass=400)
-        rows = evaluate(cfgs, load(a.model), ref_steps_per_pass=a.ref_steps, safety=a.safety)
-        tot_p = sum(r["seconds_plain"] for r in rows)
-        tot_l = sum(r["seconds_learned"] for r in rows)
-        print(json.dumps(dict(cells=len(rows), grid=grid, passes=a.passes, speedup_wall=tot_p / tot_l,
-                              max_err_plain=max(r["err_plain"] for r in rows),
-                              max_err_learned=max(r["err_learned"] for r in rows), rows=rows)))
+        safeties = tuple(float(v) for v in a.safety.split(","))
+        rows = evaluate(cfgs, load(a.model), ref_steps_per_pass=a.ref_steps, safeties=safeties)
+        summary = dict(cells=len(rows), grid=grid, passes=a.passes,
+                       plain=dict(max_err=max(r["err_plain"] for r in rows), seconds=sum(r["seconds_plain"] for r in rows)),
+                       plain_landing=dict(max_err=max(r["err_plain_landing"] for r in rows),
+                                          seconds=sum(r["seconds_plain_landing"] for r in rows)),
+                       learned={str(sf): dict(max_err=max(r["learned"][sf]["err"] for r in rows),
+                                              seconds=sum(r["learned"][sf]["seconds"] for r in rows))
+                                for sf in safeties})
+        print(json.dumps(dict(summary=summary, rows=[{k: (v if k != "learned" else {str(a): b for a, b in v.items()})
+                                                      for k, v in r.items()} for r in rows])))
     return 0
 
 

@@ -50,6 +50,7 @@ class MPCParams:
     bounce_mode: int = BOUNCE_SIGNFLIP
     roc: float = 0.0
     variant: int = 0          # compiled kernel variant of the grid (0 default, -1 autotune)
+    land_mirrors: int = 0     # step doubling ends attempts on mirror planes (0: as the reference)
 
     @property
     def Nx(self) -> int:

@@ -79,7 +79,7 @@ def test_learned_controller_beats_plain_step_doubling(gpu_lib):
     assert loss < 0.5
     cell = dzlearn.controller_cells(1000, 1, (32, 32, 256), passes=2, steps_per_pass=10, def_err=1e-4)[0]
     cell.cav = 0.1
-    rows = dzlearn.evaluate([cell], mlp, ref_steps_per_pass=400, safety=0.9, check_every=8, fallback_len=4)
+    rows = dzlearn.evaluate([cell], mlp, ref_steps_per_pass=400, safeties=(0.9,), check_every=8, fallback_len=4)
     r = rows[0]
     print(r)
     assert r["checks"] >= 1

@@ -360,3 +360,19 @@ def test_production_grids_match_oracle(gpu_lib, grid):
         prop.run_fixed(2)
         got = prop.download()
     assert rel(got, ref) < 1e-5
+
+
+def test_step_double_landing_on_mirror_planes(gpu_lib):
+    """With land_mirrors, an attempt that would cross a mirror plane ends on it: some accepted
+    state sits exactly on z = Cav, the run still reaches the next pass, and a later attempt
+    does not shrink merely because the landing step was short."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(energy=1e-3, steps_per_pass=6, def_err=1e-3)
+    with Propagator(p.copy(land_mirrors=1)) as prop:
+        prop.upload(A)
+        zs = []
+        while prop.state().z < 1.5 * p.Cav and len(zs) < 200:
+            if prop.step_double()["bad"] == 0:
+                zs.append(prop.state().z)
+        assert any(abs(z - p.Cav) < 1e-12 for z in zs), zs
+        assert zs[-1] >= 1.5 * p.Cav and np.isfinite(prop.download()).all()
