@@ -169,8 +169,8 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
-            "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror",
-                       "grid": [p.Nx, p.Ny, p.Nt], "sample": "1 split step per bench step"},
+            "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
+                       "grid": [p.Nx, p.Ny, p.Nt], "sample": "1 split step per bench step (CPU time bound)"},
             "cpu_baseline": {"value": value, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
                              "sample": "1 split step of the 256x256x2048 cell per bench step, FP64, OpenMP"},
             "e2e": {"value": value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -271,8 +271,8 @@ def run_gb300(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
                 "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
-                "config": {"workload": "multipass cell 256x256x2048, 400 fixed split steps per pass (1 pass = 1 step), "
-                                       "lens mirror, SST + ADK + plasma on", "grid": [p.Nx, p.Ny, p.Nt],
+                "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
+                           "step": "one pass of the cell = 400 split steps", "grid": [p.Nx, p.Ny, p.Nt],
                            "split_steps_per_step": STEPS_PER_PASS, "l2": "field 1 GiB > L2, no flush",
                            "parallelism": f"replicas x{world}", "kernel_variant": vinfo},
                 "roofline": roofline, "fft_rate": fft_rate, "cpu_baseline": cpu, "e2e": e2e,
