@@ -39,6 +39,7 @@ constexpr int kTilePoints = 16384;     // default pencil tile: P * Nt complex po
 #define MPC_PENCIL_UNROLL 4
 #endif
 constexpr int kPencilUnroll = MPC_PENCIL_UNROLL;
+constexpr int kDAPrefetch = 4;         // dA samples loaded ahead of use in the nonlinear walk
 
 // FP32 constants of the nonlinear step, computed on the host in FP64.
 struct NLConst {
@@ -318,11 +319,22 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             u = (float)muv[p * TPP + ch].o0;
             v = (float)muv[p * TPP + ch].o1;
         }
-        // S3: apply the nonlinear step (or emit the ionization outputs)
+        // S3: apply the nonlinear step (or emit the ionization outputs).  The dA samples come
+        // from L2: a ring of kDAPrefetch registers loads each kDAPrefetch samples ahead.
         float R = Rin;
-#pragma unroll 2
+        float2 ring[kDAPrefetch];
+        if (!IONIZ_ONLY && c.sst_c != 0.0f) {
+#pragma unroll
+            for (int k = 0; k < kDAPrefetch; k++) ring[k] = dA[k * P];
+        }
+#pragma unroll kDAPrefetch
         for (int i = 0; i < CH; i++) {
             const int t = t0 + i;
+            float2 dAi = make_float2(0.0f, 0.0f);
+            if (!IONIZ_ONLY && c.sst_c != 0.0f) {
+                dAi = ring[i % kDAPrefetch];
+                if (i + kDAPrefetch < CH) ring[i % kDAPrefetch] = dA[(i + kDAPrefetch) * P];
+            }
             const float2 a = w[V::walk(i)];
             const IonPoint ip = ion_point(a, c);
             R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
@@ -342,7 +354,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float re = -pl * ip.sigma;
             float im = fmaf(c.gam, a2, -pl * ip.qw);
             if (c.sst_c != 0.0f) {
-                const float2 sd = cmulc(dA[i * P], a);  // dA * conj(A)
+                const float2 sd = cmulc(dAi, a);  // dA * conj(A)
                 re = fmaf(-3.0f * c.sst_c, sd.x, re);
                 im = fmaf(-c.sst_c, sd.y, im);
             }
@@ -353,14 +365,21 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             mx = make_float4(fmaxf(mx.x, a2), fmaxf(mx.y, ions), fmaxf(mx.z, fabsf(im)), fmaxf(mx.w, fabsf(re)));
         }
     } else {
-#pragma unroll 4
+        float2 ring[kDAPrefetch];
+        if (c.sst_c != 0.0f) {
+#pragma unroll
+            for (int k = 0; k < kDAPrefetch; k++) ring[k] = dA[k * P];
+        }
+#pragma unroll kDAPrefetch
         for (int i = 0; i < CH; i++) {
             const float2 a = w[V::walk(i)];
             const float a2 = fmaf(a.x, a.x, a.y * a.y);
             float re = 0.0f;
             float im = c.gam * a2;
             if (c.sst_c != 0.0f) {
-                const float2 sd = cmulc(dA[i * P], a);
+                const float2 dAi = ring[i % kDAPrefetch];
+                if (i + kDAPrefetch < CH) ring[i % kDAPrefetch] = dA[(i + kDAPrefetch) * P];
+                const float2 sd = cmulc(dAi, a);
                 re = -3.0f * c.sst_c * sd.x;
                 im = fmaf(-c.sst_c, sd.y, im);
             }
