@@ -803,7 +803,9 @@ __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, cons
     dif_all<NX, NX, RV, NTHR>(s, twx, tid);
     cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
     dif_all<NY, NY, CV, NTHR>(s, twy, tid);
-    // multiply by Rx(px) and Ry(py) D(slot) (double-float factors)
+    // multiply by Rx(px) and Ry(py) D(slot) (double-float factors); unrolled so that the
+    // factors' L2 loads are in flight together
+#pragma unroll 8
     for (int e = tid; e < PB * NY * C::CX; e += NTHR) {
         const int xl = e % C::CX;
         const int r = e / C::CX;
@@ -844,6 +846,7 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_ke
     for (int unit = cid; unit < a.nunits; unit += ncl) {
         // load this CTA's rows: y in [rank*RY, rank*RY + RY) of PB planes
         constexpr int F4_ROW = NX * SLO / 2;
+#pragma unroll 8
         for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += NTHR) {
             const int c = f % F4_ROW;
             const int r = f / F4_ROW;
