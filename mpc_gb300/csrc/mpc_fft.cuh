@@ -184,6 +184,12 @@ struct Radix {
 // from the rounded values).  The forward (DIF) stage multiplies by (c, s); the inverse (DIT)
 // stage by conj(c, s) * (1 - eps), so every forward/inverse round trip has gain 1 - eps^2 per
 // path instead of 1 + eps: rounded twiddles alone lose ~6e-8 of the energy per split step.
+// In global memory the table is in natural order k; the kernels copy it to shared memory in
+// "staged" order (stage_twiddles): for each stage of sub-length L (span S = L/R) the R - 1
+// factors W_N^(j k N/L), k = 1..R-1, of every j < S, stored at [(k - 1) S + j].  The threads of
+// a warp that read one k then read consecutive words (the natural-order index j k N/L puts the
+// 4..8 j of a warp in one bank at the middle stage of a 2048-point transform), and each
+// butterfly's R - 1 addresses are one base plus compile-time offsets.
 //
 // Every view used here is "stage separable": for a butterfly of span S starting at
 // base = b*L + j (j < S), V::at(base + S*q, l) == V::at(base, l) + V::at(S*q, 0) - V::at(0, 0),
@@ -203,6 +209,41 @@ struct Twiddles {
 };
 // bytes of a packed table of N entries
 __host__ __device__ constexpr int twiddle_bytes(int N) { return N * 12; }
+
+// First entry of the stage of sub-length L in the staged table of W_N: the stages before it
+// (sub-lengths N, N/R, ...) hold L' - L'/R' entries each; all stages together hold fewer than N.
+__host__ __device__ constexpr int tw_stage_offset(int N, int L) {
+    return N == L ? 0 : (N - N / (N >= 16 ? 16 : N)) + tw_stage_offset(N / (N >= 16 ? 16 : N), L);
+}
+
+// Copy the natural-order table `src` (global) into shared memory `dst` in staged order.
+// Entries past the last stage are zero (never read).
+template <int N, int NTH>
+__device__ __forceinline__ void stage_twiddles(void* dst, const float2* __restrict__ src, int tid) {
+    float2* w = static_cast<float2*>(dst);
+    float* e = reinterpret_cast<float*>(w + N);
+    const float* se = reinterpret_cast<const float*>(src + N);
+    for (int i = tid; i < N; i += NTH) {
+        int L = N, off = 0, flat = -1;
+        while (L > 1) {
+            const int R = (L >= 16) ? 16 : L, S = L / R, cnt = L - S;
+            if (i < off + cnt) {
+                const int k = (i - off) / S + 1, j = (i - off) % S;
+                flat = j * k * (N / L);
+                break;
+            }
+            off += cnt;
+            L /= R;
+        }
+        if (flat >= 0) {
+            w[i] = __ldg(&src[flat]);
+            e[i] = __ldg(&se[flat]);
+        } else {
+            w[i] = make_float2(0.0f, 0.0f);
+            e[i] = 0.0f;
+        }
+    }
+}
 
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
 // NTH threads share the stage's TOT butterflies; UNR of a thread's butterflies are unrolled
@@ -224,9 +265,9 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid) {
         for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         dft<R, false>(v);
         if (S > 1) {
-            const float2* t = tw.w + j * (N / L);
+            const float2* t = tw.w + tw_stage_offset(N, L) + j;
 #pragma unroll
-            for (int k = 1; k < R; k++) v[k] = cmul(v[k], t[j * (k - 1) * (N / L)]);
+            for (int k = 1; k < R; k++) v[k] = cmul(v[k], t[(k - 1) * S]);
         }
 #pragma unroll
         for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
@@ -252,13 +293,13 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid) {
 #pragma unroll
         for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
         if (S > 1) {
-            const float2* t = tw.w + j * (N / L);
-            const float* te = tw.e + j * (N / L);
+            const float2* t = tw.w + tw_stage_offset(N, L) + j;
+            const float* te = tw.e + tw_stage_offset(N, L) + j;
 #pragma unroll
             for (int k = 1; k < R; k++) {
-                const float2 u = cmulc(v[k], t[j * (k - 1) * (N / L)]);
+                const float2 u = cmulc(v[k], t[(k - 1) * S]);
                 if constexpr (CORR) {
-                    const float e = te[j * (k - 1) * (N / L)];
+                    const float e = te[(k - 1) * S];
                     v[k] = make_float2(fmaf(u.x, e, u.x), fmaf(u.y, e, u.y));
                 } else {
                     v[k] = u;

@@ -551,11 +551,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
     double* tsum = reinterpret_cast<double*>(Cfg::TEMP_IN_SCAN ? smem_raw + Cfg::SMEM_FIELD : smem_raw + Cfg::SMEM);
     const int tid = threadIdx.x;
     const int NP = args.NP;
-    {
-        const float* src = reinterpret_cast<const float*>(args.tw);
-        float* dst = reinterpret_cast<float*>(tw_mem);
-        for (int k = tid; k < 3 * NT; k += TH) dst[k] = __ldg(&src[k]);
-    }
+    stage_twiddles<NT, TH>(tw_mem, args.tw, tid);
     const Twiddles tw = Twiddles::packed(tw_mem, NT);
     __syncthreads();
 
@@ -836,10 +832,8 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_ke
     const int tid = threadIdx.x;
     const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;
     const int NP = a.NP;
-    for (int k = tid; k < 3 * NX; k += NTHR)
-        reinterpret_cast<float*>(twx_mem)[k] = __ldg(&reinterpret_cast<const float*>(a.twx)[k]);
-    for (int k = tid; k < 3 * NY; k += NTHR)
-        reinterpret_cast<float*>(twy_mem)[k] = __ldg(&reinterpret_cast<const float*>(a.twy)[k]);
+    stage_twiddles<NX, NTHR>(twx_mem, a.twx, tid);
+    stage_twiddles<NY, NTHR>(twy_mem, a.twy, tid);
     const Twiddles twx = Twiddles::packed(twx_mem, NX), twy = Twiddles::packed(twy_mem, NY);
     __syncthreads();
 

@@ -152,8 +152,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     void* scan_mem = smem_raw + Cfg::SMEM_FIELD;
     unsigned char* tw_mem = smem_raw + Cfg::SMEM_FIELD + Cfg::SMEM_SCAN;
     const int tid = threadIdx.x;
-    for (int k = tid; k < 3 * NT; k += kThreads)
-        reinterpret_cast<float*>(tw_mem)[k] = reinterpret_cast<const float*>(tw_g)[k];
+    mpc::stage_twiddles<NT, kThreads>(tw_mem, tw_g, tid);
     const mpc::Twiddles tw = mpc::Twiddles::packed(tw_mem, NT);
     __syncthreads();
     float2* scr = dA_area + (size_t)blockIdx.x * NT * P;
