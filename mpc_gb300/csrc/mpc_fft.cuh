@@ -274,11 +274,21 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid) {
     }
 }
 
+// Element operations fused into an inverse transform.  PRE (active) multiplies the input
+// values in place as the first stage loads them: pre(v, pos0) gets the R values of positions
+// pos0 .. pos0 + R - 1 of one line.  SINK (active) takes the last stage's results instead of
+// shared memory: sink(v, t0, S, line) gets the values of natural indices t0 + S q, q < R.
+struct NoOp {
+    static constexpr bool active = false;
+};
+
 // DIT stage (exact transpose of the DIF stage with conjugate twiddles).  CORR = false skips the
 // (1 - eps) magnitude correction, for transforms whose result is not fed back into the field
-// (the time derivative of the self-steepening term).
-template <int N, int L, class V, int NTH, int UNR, bool CORR = true>
-__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid) {
+// (the time derivative of the self-steepening term).  The stage with span 1 (the first of the
+// inverse transform) applies PRE; the stage of sub-length N (the last) stores through SINK.
+template <int N, int L, class V, int NTH, int UNR, bool CORR = true, class PRE = NoOp, class SINK = NoOp>
+__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const PRE& pre = PRE{},
+                                          const SINK& sink = SINK{}) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -292,6 +302,7 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid) {
         float2 v[R];
 #pragma unroll
         for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
+        if constexpr (S == 1 && PRE::active) pre(v, b * L);
         if (S > 1) {
             const float2* t = tw.w + tw_stage_offset(N, L) + j;
             const float* te = tw.e + tw_stage_offset(N, L) + j;
@@ -307,8 +318,12 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid) {
             }
         }
         dft<R, true>(v);
+        if constexpr (L == N && SINK::active) {
+            sink(v, b * L + j, S, line);
+        } else {
 #pragma unroll
-        for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
+            for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
+        }
     }
 }
 
@@ -322,11 +337,12 @@ __device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid) {
 }
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
-template <int N, int L, class V, int NTH, int UNR = 1, bool CORR = true>
-__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid) {
+template <int N, int L, class V, int NTH, int UNR = 1, bool CORR = true, class PRE = NoOp, class SINK = NoOp>
+__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, const PRE& pre = PRE{},
+                                        const SINK& sink = SINK{}) {
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR>(s, tw, tid);
-    dit_stage<N, L, V, NTH, UNR, CORR>(s, tw, tid);
+    if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR, PRE, SINK>(s, tw, tid, pre, sink);
+    dit_stage<N, L, V, NTH, UNR, CORR, PRE, SINK>(s, tw, tid, pre, sink);
     __syncthreads();
 }
 

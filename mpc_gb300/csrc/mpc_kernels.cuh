@@ -503,16 +503,30 @@ __device__ __forceinline__ void load_tile_async(float2* s, const float2* __restr
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// In place: S(pos) -> -i omega(pos) S(pos), the spectrum of the time derivative.
-template <int NT, int P, int TH>
-__device__ __forceinline__ void times_minus_i_omega(float2* s, const float* __restrict__ wpos, int tid) {
-    using V = PencilView<NT, P>;
-    for (int e = tid; e < NT * P; e += TH) {
-        const int pos = e / P, p = e - (e / P) * P;
-        const int i = V::at(pos, p);
-        s[i] = cscale(mul_mi<false>(s[i]), __ldg(&wpos[pos]));
+// Fused into the first stage of the derivative's inverse transform: S(pos) -> -i omega(pos) S(pos).
+struct TimesMinusIOmega {
+    const float* __restrict__ wpos;
+    static constexpr bool active = true;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int pos0) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = cscale(mul_mi<false>(v[q]), __ldg(&wpos[pos0 + q]));
     }
-}
+};
+
+// Fused into the last stage of the derivative's inverse transform: dA(t) of pencil `line` goes
+// to the CTA's scratch tile [t][p] (L2) instead of shared memory; a warp's stores for one q
+// cover consecutive t of all P pencils.
+template <int P>
+struct ScratchSink {
+    float2* __restrict__ scr;
+    static constexpr bool active = true;
+    template <int R>
+    __device__ __forceinline__ void operator()(const float2 (&v)[R], int t0, int S, int line) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) scr[(t0 + S * q) * P + line] = v[q];
+    }
+};
 
 template <int NT, int P, int SLO, int TH>
 __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__ g, int q0, int NP, int tid) {
@@ -656,17 +670,13 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
                     load_tile_async<NT, P, TH>(s, gin, q0, NP, tid);
                     cp_async_wait_all();
                     __syncthreads();
-                    times_minus_i_omega<NT, P, TH>(s, args.wpos, tid);
+                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid, TimesMinusIOmega{args.wpos},
+                                                                  ScratchSink<P>{scr});
                 } else {
                     load_tile<NT, P, SLO, true, TH>(s, gin, args.wpos, q0, NP, tid);
+                    __syncthreads();
+                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid, NoOp{}, ScratchSink<P>{scr});
                 }
-                __syncthreads();
-                dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid);
-                for (int f = tid; f < NT * P; f += TH) {
-                    const int t = f / P, p = f - (f / P) * P;
-                    scr[f] = s[V::at(t, p)];
-                }
-                __syncthreads();
             }
             // A = IFFT_t(S)
             if constexpr (SLO == 1) {
