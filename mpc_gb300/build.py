@@ -16,7 +16,7 @@ SOURCES = ["mpc_capi.cu", "mpc_shapes_a.cu", "mpc_shapes_b.cu", "mpc_shapes_c.cu
            "mpc_noalloc.cu", "mpc_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
-# extra defines for tuning builds, e.g. MPC_NVCC_EXTRA="-DMPC_PREFETCH=0"
+# extra defines for tuning builds, e.g. MPC_NVCC_EXTRA="-DMPC_PENCIL_UNROLL=2"
 FLAGS += os.environ.get("MPC_NVCC_EXTRA", "").split()
 
 

@@ -245,11 +245,20 @@ __device__ __forceinline__ void stage_twiddles(void* dst, const float2* __restri
     }
 }
 
+// Loads and stores fused into a transform's first or last stage, in place of shared memory.
+// A SRC (active) gives the first stage of an inverse transform its inputs: src(v, pos0, line)
+// fills v with positions pos0 .. pos0 + R - 1 of one line.  A SINK (active) takes the results
+// of the last stage: sink(v, i0, S, line) gets indices i0 + S q, q < R (natural order after an
+// inverse transform, position order after a forward one, where S = 1).
+struct NoOp {
+    static constexpr bool active = false;
+};
+
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
 // NTH threads share the stage's TOT butterflies; UNR of a thread's butterflies are unrolled
 // together so that their shared-memory loads overlap.
-template <int N, int L, class V, int NTH, int UNR>
-__device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid) {
+template <int N, int L, class V, int NTH, int UNR, class SINK = NoOp>
+__device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, const SINK& sink = SINK{}) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
     constexpr int NB = N / R;
@@ -269,25 +278,21 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid) {
 #pragma unroll
             for (int k = 1; k < R; k++) v[k] = cmul(v[k], t[(k - 1) * S]);
         }
+        if constexpr (S == 1 && SINK::active) {
+            sink(v, b * L, 1, line);
+        } else {
 #pragma unroll
-        for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
+            for (int q = 0; q < R; q++) p0[V::at(S * q, 0) - V::at(0, 0)] = v[q];
+        }
     }
 }
-
-// Element operations fused into an inverse transform.  PRE (active) multiplies the input
-// values in place as the first stage loads them: pre(v, pos0) gets the R values of positions
-// pos0 .. pos0 + R - 1 of one line.  SINK (active) takes the last stage's results instead of
-// shared memory: sink(v, t0, S, line) gets the values of natural indices t0 + S q, q < R.
-struct NoOp {
-    static constexpr bool active = false;
-};
 
 // DIT stage (exact transpose of the DIF stage with conjugate twiddles).  CORR = false skips the
 // (1 - eps) magnitude correction, for transforms whose result is not fed back into the field
 // (the time derivative of the self-steepening term).  The stage with span 1 (the first of the
-// inverse transform) applies PRE; the stage of sub-length N (the last) stores through SINK.
-template <int N, int L, class V, int NTH, int UNR, bool CORR = true, class PRE = NoOp, class SINK = NoOp>
-__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const PRE& pre = PRE{},
+// inverse transform) loads through SRC; the stage of sub-length N (the last) stores through SINK.
+template <int N, int L, class V, int NTH, int UNR, bool CORR = true, class SRC = NoOp, class SINK = NoOp>
+__device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const SRC& src = SRC{},
                                           const SINK& sink = SINK{}) {
     constexpr int R = Radix<L>::R;
     constexpr int S = L / R;
@@ -300,9 +305,12 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const
         const int b = g / S, j = g - (g / S) * S;
         float2* p0 = s + V::at(b * L + j, line);
         float2 v[R];
+        if constexpr (S == 1 && SRC::active) {
+            src(v, b * L, line);
+        } else {
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
-        if constexpr (S == 1 && PRE::active) pre(v, b * L);
+            for (int q = 0; q < R; q++) v[q] = p0[V::at(S * q, 0) - V::at(0, 0)];
+        }
         if (S > 1) {
             const float2* t = tw.w + tw_stage_offset(N, L) + j;
             const float* te = tw.e + tw_stage_offset(N, L) + j;
@@ -328,22 +336,56 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const
 }
 
 // Whole forward transform (natural -> position order).  Ends with a __syncthreads.
-template <int N, int L, class V, int NTH, int UNR = 1>
-__device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid) {
-    dif_stage<N, L, V, NTH, UNR>(s, tw, tid);
+template <int N, int L, class V, int NTH, int UNR = 1, class SINK = NoOp>
+__device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid, const SINK& sink = SINK{}) {
+    dif_stage<N, L, V, NTH, UNR, SINK>(s, tw, tid, sink);
     __syncthreads();
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dif_all<N, L / R, V, NTH, UNR>(s, tw, tid);
+    if constexpr (L / R > 1) dif_all<N, L / R, V, NTH, UNR, SINK>(s, tw, tid, sink);
 }
 
 // Whole inverse transform (position -> natural order), unnormalised.  Ends with a sync.
-template <int N, int L, class V, int NTH, int UNR = 1, bool CORR = true, class PRE = NoOp, class SINK = NoOp>
-__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, const PRE& pre = PRE{},
+template <int N, int L, class V, int NTH, int UNR = 1, bool CORR = true, class SRC = NoOp, class SINK = NoOp>
+__device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, const SRC& src = SRC{},
                                         const SINK& sink = SINK{}) {
     constexpr int R = Radix<L>::R;
-    if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR, PRE, SINK>(s, tw, tid, pre, sink);
-    dit_stage<N, L, V, NTH, UNR, CORR, PRE, SINK>(s, tw, tid, pre, sink);
+    if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR, SRC, SINK>(s, tw, tid, src, sink);
+    dit_stage<N, L, V, NTH, UNR, CORR, SRC, SINK>(s, tw, tid, src, sink);
     __syncthreads();
+}
+
+// Forward transform, a diagonal operator in position order, inverse transform: the span-1 stage
+// of the forward transform, the operator and the span-1 stage of the inverse work on the same R
+// positions of a line, so they run in registers in one pass (op(v, pos0, line) multiplies the
+// values of positions pos0 .. pos0 + R - 1).  Same arithmetic as dif_all, a pass applying op,
+// then dit_all.  Ends with a __syncthreads.
+template <int N, int L, class V, int NTH, int UNR, class OP>
+__device__ __forceinline__ void dif_op_dit(float2* s, Twiddles tw, int tid, const OP& op) {
+    constexpr int R = Radix<L>::R;
+    if constexpr (L / R > 1) {
+        dif_stage<N, L, V, NTH, UNR>(s, tw, tid);
+        __syncthreads();
+        dif_op_dit<N, L / R, V, NTH, UNR, OP>(s, tw, tid, op);
+        dit_stage<N, L, V, NTH, UNR>(s, tw, tid);
+        __syncthreads();
+    } else {
+        constexpr int TOT = (N / R) * V::NLINES;
+#pragma unroll UNR
+        for (int idx = tid; idx < TOT; idx += NTH) {
+            const int line = idx % V::NLINES;
+            const int b = idx / V::NLINES;
+            float2* p0 = s + V::at(b * L, line);
+            float2 v[R];
+#pragma unroll
+            for (int q = 0; q < R; q++) v[q] = p0[V::at(q, 0) - V::at(0, 0)];
+            dft<R, false>(v);
+            op(v, b * L, line);
+            dft<R, true>(v);
+#pragma unroll
+            for (int q = 0; q < R; q++) p0[V::at(q, 0) - V::at(0, 0)] = v[q];
+        }
+        __syncthreads();
+    }
 }
 
 }  // namespace mpc

@@ -26,12 +26,6 @@ namespace cg = cooperative_groups;
 namespace mpc {
 
 constexpr int kThreads = 512;          // threads of a one-CTA-per-SM launch (128 registers each)
-// L2 prefetch of the next pencil tile: measured slower on GB300 (it evicts the dA scratch
-// tiles from L2), so off by default
-#ifndef MPC_PREFETCH
-#define MPC_PREFETCH 0
-#endif
-constexpr bool kPrefetch = MPC_PREFETCH != 0;
 constexpr int kTilePoints = 16384;     // default pencil tile: P * Nt complex points (128 KB)
 // butterflies of a pencil thread unrolled together per FFT stage (the plane sweep keeps 1: its
 // kernels are at the register limit)
@@ -436,18 +430,6 @@ struct PencilCfg {
     static_assert((P * SLO) % 2 == 0, "rows must be whole float4s");
 };
 
-// L2 prefetch of the P*SLO*8 = 128 B rows of a slot-layout tile (overlaps the next tile's
-// DRAM reads with this tile's compute; one bulk prefetch per row)
-template <int NT, int P, int SLO, int TH>
-__device__ __forceinline__ void prefetch_tile(const float2* g, int q0, int NP, int tid) {
-    constexpr int ROWS = NT / SLO;
-    constexpr int BYTES = P * SLO * 8;
-    for (int row = tid; row < ROWS; row += TH) {
-        const float2* a = g + ((size_t)row * NP + q0) * SLO;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "n"(BYTES) : "memory");
-    }
-}
-
 // Element order of the two complex values of a float4 row chunk.  For SLO = 2 the pair is
 // (pos 2r, pos 2r + 1) of one pencil; odd rows store them in the opposite order so that
 // the four rows a warp touches fall on both halves of the shared-memory banks.
@@ -482,11 +464,16 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
     }
 }
 
+// Slot-layout index of spectrum position pos of pencil q (a multiple-of-P tile start plus line)
+template <int SLO>
+__device__ __forceinline__ size_t slot_index(int pos, int q, int NP) {
+    return ((size_t)(pos / SLO) * NP + q) * SLO + (pos % SLO);
+}
+
 // Asynchronous tile load for the SLO = 1 layout: every 16 B chunk of a t-row (pencils 2c and
 // 2c + 1 at one position) is copied from global to shared memory by cp.async, all of them in
-// flight at once instead of each thread waiting on its loads in turn.  Both addresses are 16 B
-// aligned: NP and q0 are even, and P and the view's pad are even.  The caller waits with
-// cp_async_wait_all() and synchronises the CTA before using the tile.
+// flight at once.  Both addresses are 16 B aligned: NP and q0 are even, and P and the view's
+// pad are even.  Ends with the wait and a CTA barrier.
 template <int NT, int P, int TH>
 __device__ __forceinline__ void load_tile_async(float2* s, const float2* __restrict__ g, int q0, int NP, int tid) {
     using V = PencilView<NT, P>;
@@ -500,17 +487,67 @@ __device__ __forceinline__ void load_tile_async(float2* s, const float2* __restr
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Fused into the first stage of the derivative's inverse transform: S(pos) -> -i omega(pos) S(pos).
-struct TimesMinusIOmega {
+// The tile's spectrum into shared memory (pencil view), then a CTA barrier.
+template <int NT, int P, int SLO, int TH>
+__device__ __forceinline__ void stage_tile(float2* s, const float2* __restrict__ g, int q0, int NP, int tid) {
+    if constexpr (SLO == 1) {
+        load_tile_async<NT, P, TH>(s, g, q0, NP, tid);
+    } else {
+        load_tile<NT, P, SLO, false, TH>(s, g, nullptr, q0, NP, tid);
+        __syncthreads();
+    }
+}
+
+// First stage of the derivative's inverse t transform over a staged tile: S(pos) from shared
+// memory times -i omega(pos).
+template <class V>
+struct SmemDerivSource {
+    const float2* s;
     const float* __restrict__ wpos;
     static constexpr bool active = true;
     template <int R>
-    __device__ __forceinline__ void operator()(float2 (&v)[R], int pos0) const {
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int pos0, int line) const {
+        const float2* p0 = s + V::at(pos0, line);
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = cscale(mul_mi<false>(v[q]), __ldg(&wpos[pos0 + q]));
+        for (int q = 0; q < R; q++) v[q] = cscale(mul_mi<false>(p0[V::at(q, 0) - V::at(0, 0)]), __ldg(&wpos[pos0 + q]));
+    }
+};
+
+// First stage of an inverse t transform reading the tile's spectrum straight from global memory
+// (through L2: the tile is read twice per step and written once, by this CTA only); DERIV
+// multiplies by -i omega(pos), the spectrum of the time derivative.  A warp's loads for one q
+// are P-pencil row segments of 8 positions.
+template <int P, int SLO, bool DERIV>
+struct TileSource {
+    const float2* __restrict__ g;
+    const float* __restrict__ wpos;
+    int q0, NP;
+    static constexpr bool active = true;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int pos0, int line) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = __ldcg(&g[slot_index<SLO>(pos0 + q, q0 + line, NP)]);
+        if constexpr (DERIV) {
+#pragma unroll
+            for (int q = 0; q < R; q++) v[q] = cscale(mul_mi<false>(v[q]), __ldg(&wpos[pos0 + q]));
+        }
+    }
+};
+
+// Last stage of the forward t transform writing the tile's spectrum to global memory.
+template <int P, int SLO>
+struct TileSink {
+    float2* __restrict__ g;
+    int q0, NP;
+    static constexpr bool active = true;
+    template <int R>
+    __device__ __forceinline__ void operator()(const float2 (&v)[R], int pos0, int S, int line) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) g[slot_index<SLO>(pos0 + S * q, q0 + line, NP)] = v[q];
     }
 };
 
@@ -552,7 +589,9 @@ __device__ __forceinline__ void store_tile(const float2* s, float2* __restrict__
     }
 }
 
-template <int NT, int P, int SLO, int MODE, int CH = 32>
+// LD: how the split step reads the tile (0: staged in shared memory by cp.async, best with
+// 32 B t-rows; 1: loaded by the first transform stages, best with 64 B and wider rows).
+template <int NT, int P, int SLO, int MODE, int CH = 32, int LD = 1>
 __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, P, SLO, CH>::TH >= kThreads ? 1 : 2))
     pencil_kernel(PencilArgs args) {
     using Cfg = PencilCfg<NT, P, SLO, CH>;
@@ -577,11 +616,6 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
 
     for (int tile = blockIdx.x; tile < args.ntiles; tile += gridDim.x) {
         const int q0 = tile * P;
-        if constexpr (kPrefetch && (MODE == PM_STEP || MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP)) {
-            const int nxt = tile + gridDim.x;
-            if (nxt < args.ntiles)
-                prefetch_tile<NT, P, SLO, TH>(reinterpret_cast<const float2*>(args.in), nxt * P, NP, tid);
-        }
         if constexpr (MODE == PM_IONIZ) {
             for (int f = tid; f < NT * P; f += TH) {
                 const int t = f / P, p = f - (f / P) * P;
@@ -665,34 +699,29 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
             float2* scr = args.scratch + (size_t)blockIdx.x * NT * P;
             // dA = IFFT_t(-i omega S): the time derivative of the self-steepening term, kept in
             // this CTA's scratch tile [t][p] (L2-resident) until the nonlinear walk
+            // (LD = 1: the transforms' first stages load the spectrum from global memory; LD = 0:
+            // it is staged in shared memory by bulk asynchronous copies first)
             if (c.sst_c != 0.0f) {
-                if constexpr (SLO == 1) {
-                    load_tile_async<NT, P, TH>(s, gin, q0, NP, tid);
-                    cp_async_wait_all();
-                    __syncthreads();
-                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid, TimesMinusIOmega{args.wpos},
-                                                                  ScratchSink<P>{scr});
+                if constexpr (LD == 1) {
+                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(
+                        s, tw, tid, TileSource<P, SLO, true>{gin, args.wpos, q0, NP}, ScratchSink<P>{scr});
                 } else {
-                    load_tile<NT, P, SLO, true, TH>(s, gin, args.wpos, q0, NP, tid);
-                    __syncthreads();
-                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid, NoOp{}, ScratchSink<P>{scr});
+                    stage_tile<NT, P, SLO, TH>(s, gin, q0, NP, tid);
+                    dit_all<NT, NT, V, TH, kPencilUnroll, false>(s, tw, tid, SmemDerivSource<V>{s, args.wpos},
+                                                                  ScratchSink<P>{scr});
                 }
             }
             // A = IFFT_t(S)
-            if constexpr (SLO == 1) {
-                load_tile_async<NT, P, TH>(s, gin, q0, NP, tid);
-                cp_async_wait_all();
+            if constexpr (LD == 1) {
+                dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid, TileSource<P, SLO, false>{gin, args.wpos, q0, NP});
             } else {
-                load_tile<NT, P, SLO, false, TH>(s, gin, args.wpos, q0, NP, tid);
+                stage_tile<NT, P, SLO, TH>(s, gin, q0, NP, tid);
+                dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             }
-            __syncthreads();
-            dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
 
             nonlinear_tile<NT, P, false, CH>(s, scr, c, scan_mem, tid, nullptr, nullptr, q0, NP, mx);
             __syncthreads();
-            dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
-            store_tile<NT, P, SLO, TH>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
-            __syncthreads();
+            dif_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid, TileSink<P, SLO>{reinterpret_cast<float2*>(args.out), q0, NP});
         }
     }
     if constexpr (MODE == PM_TEMP) {
@@ -800,6 +829,23 @@ __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& c
     }
 }
 
+// The linear step's factors at column-view positions: line l = pl * CX + xl is column
+// px = rank * CX + xl of plane pl of the unit; positions are y (FFT position order).
+template <int CX, int SLO, int PB>
+struct PlaneFactors {
+    const PlaneTables& T;
+    int Nt, rank, unit;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int y0, int line) const {
+        const int pl = line / CX, xl = line - pl * CX;
+        const float4 rx = __ldg(&T.Rx[rank * CX + xl]);
+        const int slot = (SLO == 1) ? unit * PB + pl : unit * SLO + pl;
+        const float4* ryd = T.RyD + (size_t)y0 * Nt + slot;
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = cmul_df(cmul_df(v[q], rx), __ldg(&ryd[(size_t)q * Nt]));
+    }
+};
+
 template <int NX, int NY, int CL, int PB, int SLO, int NTHR>
 __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, const PlaneTables& T, int rank, int unit,
                                              Twiddles twx, Twiddles twy, cg::cluster_group& cluster, int tid) {
@@ -808,21 +854,8 @@ __device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, cons
     using CV = ColView<NX, NY, CL, PB, SLO>;
     dif_all<NX, NX, RV, NTHR>(s, twx, tid);
     cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
-    dif_all<NY, NY, CV, NTHR>(s, twy, tid);
-    // multiply by Rx(px) and Ry(py) D(slot) (double-float factors); unrolled so that the
-    // factors' L2 loads are in flight together
-#pragma unroll 8
-    for (int e = tid; e < PB * NY * C::CX; e += NTHR) {
-        const int xl = e % C::CX;
-        const int r = e / C::CX;
-        const int y = r % NY, pl = r / NY;
-        const int px = rank * C::CX + xl;
-        const int slot = (SLO == 1) ? unit * PB + pl : unit * SLO + pl;
-        const int idx = CV::at(y, pl * C::CX + xl);
-        s[idx] = cmul_df(cmul_df(s[idx], __ldg(&T.Rx[px])), __ldg(&T.RyD[(size_t)y * a.Nt + slot]));
-    }
-    __syncthreads();
-    dit_all<NY, NY, CV, NTHR>(s, twy, tid);
+    // FFT_y, multiply by Rx(px) Ry(py) D(slot) (double-float factors), IFFT_y
+    dif_op_dit<NY, NY, CV, NTHR, 1>(s, twy, tid, PlaneFactors<C::CX, SLO, PB>{T, a.Nt, rank, unit});
     cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
     dit_all<NX, NX, RV, NTHR>(s, twx, tid);
 }

@@ -5,6 +5,7 @@
 //                nonlinear walk (TP = 16384, CH = 32: one 512-thread CTA per SM; TP = 8192: two
 //                256-thread CTAs per SM; TP = 16384, CH = 16: one 1024-thread CTA per SM);
 //   SLO          slots interleaved in the layout (default 2 when P = 8, so t-rows are 128 B);
+//   LD           how the split-step pencil pass reads a tile (pencil_kernel);
 //   plane unit   PT threads per CTA and 512 / PT CTAs per SM, each CTA holding a
 //                PLB = 128 KB * PT / 512 share of the unit; SLO == 2: the two interleaved
 //                omega-planes split over CL CTAs; SLO == 1: planes larger than PLB split over
@@ -18,7 +19,7 @@
 namespace mpc {
 
 struct ShapeOps {
-    int Nx, Ny, Nt, P, SLO, CL, PB, PT, CH;
+    int Nx, Ny, Nt, P, SLO, CL, PB, PT, CH, LD;
     int pencil_smem, plane_smem;
     cudaError_t (*setup)();
     cudaError_t (*pencil)(int mode, const PencilArgs&, int grid, cudaStream_t);
@@ -27,7 +28,7 @@ struct ShapeOps {
     int (*pencil_blocks_per_sm)();   // resident split-step pencil CTAs per SM
 };
 
-template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints, int CH = 32>
+template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints, int CH = 32, int LD = 1>
 struct Shape {
     static constexpr int P = TP / NT;
     static constexpr int SLO = SLO_ > 0 ? SLO_ : ((P < 16) ? 16 / P : 1);
@@ -48,13 +49,13 @@ struct Shape {
 #define MPC_SET_SMEM(K, B)                                                                       \
     e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, B);                   \
     if (e != cudaSuccess) return e;
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C128, CH>), PC::smem(PM_ENTRY_C128));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C64, CH>), PC::smem(PM_ENTRY_C64));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_STEP, CH>), PC::smem(PM_STEP));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C128, CH>), PC::smem(PM_EXIT_C128));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH>), PC::smem(PM_EXIT_C64));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP, CH>), PC::smem(PM_TEMP));
-        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ, CH>), PC::smem(PM_IONIZ));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C128, CH, LD>), PC::smem(PM_ENTRY_C128));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_ENTRY_C64, CH, LD>), PC::smem(PM_ENTRY_C64));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_STEP, CH, LD>), PC::smem(PM_STEP));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C128, CH, LD>), PC::smem(PM_EXIT_C128));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH, LD>), PC::smem(PM_EXIT_C64));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP, CH, LD>), PC::smem(PM_TEMP));
+        MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ, CH, LD>), PC::smem(PM_IONIZ));
         MPC_SET_SMEM((plane_kernel<NX, NY, CL, PB, SLO, PT>), LC::SMEM);
 #undef MPC_SET_SMEM
         if (CL > 8) {
@@ -67,13 +68,13 @@ struct Shape {
 
     static cudaError_t pencil(int mode, const PencilArgs& a, int grid, cudaStream_t st) {
         switch (mode) {
-            case PM_ENTRY_C128: pencil_kernel<NT, P, SLO, PM_ENTRY_C128, CH><<<grid, TH, PC::smem(PM_ENTRY_C128), st>>>(a); break;
-            case PM_ENTRY_C64: pencil_kernel<NT, P, SLO, PM_ENTRY_C64, CH><<<grid, TH, PC::smem(PM_ENTRY_C64), st>>>(a); break;
-            case PM_STEP: pencil_kernel<NT, P, SLO, PM_STEP, CH><<<grid, TH, PC::smem(PM_STEP), st>>>(a); break;
-            case PM_EXIT_C128: pencil_kernel<NT, P, SLO, PM_EXIT_C128, CH><<<grid, TH, PC::smem(PM_EXIT_C128), st>>>(a); break;
-            case PM_EXIT_C64: pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH><<<grid, TH, PC::smem(PM_EXIT_C64), st>>>(a); break;
-            case PM_TEMP: pencil_kernel<NT, P, SLO, PM_TEMP, CH><<<grid, TH, PC::smem(PM_TEMP), st>>>(a); break;
-            case PM_IONIZ: pencil_kernel<NT, P, SLO, PM_IONIZ, CH><<<grid, TH, PC::smem(PM_IONIZ), st>>>(a); break;
+            case PM_ENTRY_C128: pencil_kernel<NT, P, SLO, PM_ENTRY_C128, CH, LD><<<grid, TH, PC::smem(PM_ENTRY_C128), st>>>(a); break;
+            case PM_ENTRY_C64: pencil_kernel<NT, P, SLO, PM_ENTRY_C64, CH, LD><<<grid, TH, PC::smem(PM_ENTRY_C64), st>>>(a); break;
+            case PM_STEP: pencil_kernel<NT, P, SLO, PM_STEP, CH, LD><<<grid, TH, PC::smem(PM_STEP), st>>>(a); break;
+            case PM_EXIT_C128: pencil_kernel<NT, P, SLO, PM_EXIT_C128, CH, LD><<<grid, TH, PC::smem(PM_EXIT_C128), st>>>(a); break;
+            case PM_EXIT_C64: pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH, LD><<<grid, TH, PC::smem(PM_EXIT_C64), st>>>(a); break;
+            case PM_TEMP: pencil_kernel<NT, P, SLO, PM_TEMP, CH, LD><<<grid, TH, PC::smem(PM_TEMP), st>>>(a); break;
+            case PM_IONIZ: pencil_kernel<NT, P, SLO, PM_IONIZ, CH, LD><<<grid, TH, PC::smem(PM_IONIZ), st>>>(a); break;
             default: return cudaErrorInvalidValue;
         }
         return cudaGetLastError();
@@ -114,14 +115,14 @@ struct Shape {
 
     static int pencil_blocks_per_sm() {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pencil_kernel<NT, P, SLO, PM_STEP, CH>, TH, PC::SMEM) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pencil_kernel<NT, P, SLO, PM_STEP, CH, LD>, TH, PC::SMEM) !=
             cudaSuccess)
             return 0;
         return n;
     }
 
     static const ShapeOps* ops() {
-        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PT, CH, PC::SMEM, LC::SMEM, &setup, &pencil, &plane,
+        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PT, CH, LD, PC::SMEM, LC::SMEM, &setup, &pencil, &plane,
                                    &max_clusters, &pencil_blocks_per_sm};
         return &o;
     }

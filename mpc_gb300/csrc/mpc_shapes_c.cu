@@ -6,7 +6,8 @@
 namespace mpc {
 extern const ShapeOps* const shape_list_c[];
 const ShapeOps* const shape_list_c[] = {
-    Shape<256,256,2048,1,256,8192>::ops(), // SLO 1, 4-pencil tiles, 256-thread pencil and plane CTAs
+    Shape<256,256,2048,1,256,8192,32,0>::ops(),  // SLO 1, 4-pencil tiles staged by cp.async, 256-thread
+                                                 // pencil and plane CTAs
     Shape<256,256,2048,1,256>::ops(),      // SLO 1, 8-pencil tiles (512 threads), plane as above
     Shape<256,256,2048>::ops(),            // SLO 2, plane 512 threads, clusters of 8 (2 planes)
     Shape<256,256,2048,1,512>::ops(),      // SLO 1, plane 512 threads, clusters of 4
