@@ -11,9 +11,10 @@
 //   IFFT_t of -i*omega*S -> dA,  IFFT_t of S -> A,  nonlinear step N(dz) (Kerr, self-
 //   steepening, ADK ionization with two affine prefix scans along t, plasma absorption and
 //   defocusing, A *= exp(dz*A_nl)),  FFT_t -> S.
-// Sweep 2, plane pass (one thread-block cluster per SLO omega-planes):
-//   FFT_x, FFT_y, multiply by Rx(kx) Ry(ky) D(omega) / (Nx Ny Nt), IFFT_y, IFFT_x; rows
-//   and columns move between the cluster's CTAs through distributed shared memory.
+// Sweep 2, plane pass (one thread-block cluster per unit of omega-planes):
+//   FFT_y, Ry(ky) D(omega) / (Nx Ny Nt), IFFT_y on columns, then FFT_x, Rx(kx), IFFT_x on
+//   rows; the columns become rows in one exchange between the cluster's CTAs through
+//   distributed shared memory.
 #pragma once
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -829,43 +830,96 @@ __device__ __forceinline__ void cluster_exchange(float2* s, cg::cluster_group& c
     }
 }
 
-// The linear step's factors at column-view positions: line l = pl * CX + xl is column
-// px = rank * CX + xl of plane pl of the unit; positions are y (FFT position order).
+// Ry(py) D(slot) (double-float) at column-view positions y (FFT position order) of line
+// l = pl * CX + xl, plane pl of the unit.
 template <int CX, int SLO, int PB>
-struct PlaneFactors {
-    const PlaneTables& T;
-    int Nt, rank, unit;
+struct YFactors {
+    const float4* __restrict__ RyD;
+    int Nt, unit;
     template <int R>
     __device__ __forceinline__ void operator()(float2 (&v)[R], int y0, int line) const {
-        const int pl = line / CX, xl = line - pl * CX;
-        const float4 rx = __ldg(&T.Rx[rank * CX + xl]);
+        const int pl = line / CX;
         const int slot = (SLO == 1) ? unit * PB + pl : unit * SLO + pl;
-        const float4* ryd = T.RyD + (size_t)y0 * Nt + slot;
+        const float4* f = RyD + (size_t)y0 * Nt + slot;
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = cmul_df(cmul_df(v[q], rx), __ldg(&ryd[(size_t)q * Nt]));
+        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], __ldg(&f[(size_t)q * Nt]));
+    }
+};
+// Rx(px) (double-float) at row-view positions x (FFT position order).
+struct XFactors {
+    const float4* __restrict__ Rx;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int x0, int) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], __ldg(&Rx[x0 + q]));
     }
 };
 
-template <int NX, int NY, int CL, int PB, int SLO, int NTHR>
-__device__ __forceinline__ void plane_linear(float2* s, const PlaneArgs& a, const PlaneTables& T, int rank, int unit,
-                                             Twiddles twx, Twiddles twy, cg::cluster_group& cluster, int tid) {
+// Move this CTA's share of a unit between global and shared memory: ROWS, the rows
+// y in [rank RY, rank RY + RY) (row view, NX * 8 B contiguous per row and plane); otherwise
+// the columns x in [rank CX, rank CX + CX) of every row (column view, CX * 8 B per row and
+// plane).  STORE: shared -> global.  SLO == 2: one float4 holds both slots of one x.
+template <int NX, int NY, int CL, int PB, int SLO, int NTHR, bool ROWS, bool STORE>
+__device__ __forceinline__ void plane_move(float2* s, const float2* __restrict__ gin, float2* __restrict__ gout,
+                                           int rank, int unit, int NP, int tid) {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
     using CV = ColView<NX, NY, CL, PB, SLO>;
-    dif_all<NX, NX, RV, NTHR>(s, twx, tid);
-    cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
-    // FFT_y, multiply by Rx(px) Ry(py) D(slot) (double-float factors), IFFT_y
-    dif_op_dit<NY, NY, CV, NTHR, 1>(s, twy, tid, PlaneFactors<C::CX, SLO, PB>{T, a.Nt, rank, unit});
-    cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
-    dit_all<NX, NX, RV, NTHR>(s, twx, tid);
+    constexpr int W = ROWS ? NX : C::CX;    // x extent moved per row
+    constexpr int NR = ROWS ? C::RY : NY;   // rows moved per plane block
+    static_assert((W * SLO) % 2 == 0, "rows move as float4");
+    constexpr int F4_ROW = W * SLO / 2;
+    const int x0 = ROWS ? 0 : rank * C::CX;
+    const int y0 = ROWS ? rank * C::RY : 0;
+#pragma unroll 8
+    for (int f = tid; f < PB / SLO * NR * F4_ROW; f += NTHR) {
+        const int c = f % F4_ROW;
+        const int r = f / F4_ROW;
+        const int yr = r % NR, plb = r / NR;  // plb: plane block (SLO == 1: plane)
+        const int y = y0 + yr;
+        size_t gi;
+        int i0, i1;
+        if constexpr (SLO == 1) {
+            gi = ((size_t)(unit * PB + plb) * NP + (size_t)y * NX + x0) / 2 + c;
+            if constexpr (ROWS) {
+                i0 = RV::at(2 * c, plb * C::RY + yr);
+                i1 = RV::at(2 * c + 1, plb * C::RY + yr);
+            } else {
+                i0 = CV::at(y, plb * C::CX + 2 * c);
+                i1 = CV::at(y, plb * C::CX + 2 * c + 1);
+            }
+        } else {
+            gi = (size_t)unit * NP + (size_t)y * NX + x0 + c;
+            if constexpr (ROWS) {
+                i0 = RV::at(c, yr);
+                i1 = RV::at(c, C::RY + yr);
+            } else {
+                i0 = CV::at(y, c);
+                i1 = CV::at(y, C::CX + c);
+            }
+        }
+        if constexpr (STORE) {
+            const float2 e0 = s[i0], e1 = s[i1];
+            reinterpret_cast<float4*>(gout)[gi] = make_float4(e0.x, e0.y, e1.x, e1.y);
+        } else {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(gin) + gi);
+            s[i0] = make_float2(v.x, v.y);
+            s[i1] = make_float2(v.z, v.w);
+        }
+    }
 }
 
 // NTHR threads per CTA; 512 / NTHR CTAs per SM (the register file holds 512 threads at
-// 128 registers).
+// 128 registers).  The linear step factorises, IFFT_xy Rx Ry D FFT_xy =
+// (IFFT_x Rx FFT_x)(IFFT_y Ry D FFT_y), so a unit is loaded by columns, takes its y part in
+// the column view, moves to the row view in one cluster exchange, takes its x part and is
+// stored by rows.  With the mirror lens: y(t1), exchange, x(t1), lens, x(t2), exchange,
+// y(t2), stored by columns.
 template <int NX, int NY, int CL, int PB, int SLO, int NTHR>
 __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_kernel(PlaneArgs a) {
     using C = PlaneCfg<NX, NY, CL, PB, SLO>;
     using RV = RowView<NX, NY, CL, PB, SLO>;
+    using CV = ColView<NX, NY, CL, PB, SLO>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
     unsigned char* twx_mem = smem_raw + C::SIZE * 8;
@@ -881,30 +935,11 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_ke
     __syncthreads();
 
     for (int unit = cid; unit < a.nunits; unit += ncl) {
-        // load this CTA's rows: y in [rank*RY, rank*RY + RY) of PB planes
-        constexpr int F4_ROW = NX * SLO / 2;
-#pragma unroll 8
-        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += NTHR) {
-            const int c = f % F4_ROW;
-            const int r = f / F4_ROW;
-            const int yl = r % C::RY, plb = r / C::RY;  // plb: plane block (SLO == 1: plane)
-            const int y = rank * C::RY + yl;
-            size_t gi;
-            if constexpr (SLO == 1) gi = ((size_t)(unit * PB + plb) * NP + (size_t)y * NX) / 2 + c;
-            else gi = ((size_t)unit * NP * SLO + (size_t)y * NX * SLO) / 2 + c;
-            const float4 v = __ldg(reinterpret_cast<const float4*>(a.in) + gi);
-            if constexpr (SLO == 1) {
-                const int x = 2 * c;
-                s[RV::at(x, plb * C::RY + yl)] = make_float2(v.x, v.y);
-                s[RV::at(x + 1, plb * C::RY + yl)] = make_float2(v.z, v.w);
-            } else {
-                const int x = c;  // one float4 = both slots of one x
-                s[RV::at(x, 0 * C::RY + yl)] = make_float2(v.x, v.y);
-                s[RV::at(x, 1 * C::RY + yl)] = make_float2(v.z, v.w);
-            }
-        }
+        plane_move<NX, NY, CL, PB, SLO, NTHR, false, false>(s, a.in, nullptr, rank, unit, NP, tid);
         __syncthreads();
-        plane_linear<NX, NY, CL, PB, SLO, NTHR>(s, a, a.t1, rank, unit, twx, twy, cluster, tid);
+        dif_op_dit<NY, NY, CV, NTHR, 1>(s, twy, tid, YFactors<C::CX, SLO, PB>{a.t1.RyD, a.Nt, unit});
+        cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
+        dif_op_dit<NX, NX, RV, NTHR, 1>(s, twx, tid, XFactors{a.t1.Rx});
         if (a.lens) {
             // mirror lens in real (x, y): exp(-i k0 (x^2 + y^2)/roc) = lensx[x] * lensy[y]
             for (int e = tid; e < PB * C::RY * NX; e += NTHR) {
@@ -916,26 +951,12 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_ke
                 s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y])));
             }
             __syncthreads();
-            plane_linear<NX, NY, CL, PB, SLO, NTHR>(s, a, a.t2, rank, unit, twx, twy, cluster, tid);
-        }
-        for (int f = tid; f < PB / SLO * C::RY * F4_ROW; f += NTHR) {
-            const int c = f % F4_ROW;
-            const int r = f / F4_ROW;
-            const int yl = r % C::RY, plb = r / C::RY;
-            const int y = rank * C::RY + yl;
-            size_t gi;
-            if constexpr (SLO == 1) gi = ((size_t)(unit * PB + plb) * NP + (size_t)y * NX) / 2 + c;
-            else gi = ((size_t)unit * NP * SLO + (size_t)y * NX * SLO) / 2 + c;
-            float2 e0, e1;
-            if constexpr (SLO == 1) {
-                const int x = 2 * c;
-                e0 = s[RV::at(x, plb * C::RY + yl)];
-                e1 = s[RV::at(x + 1, plb * C::RY + yl)];
-            } else {
-                e0 = s[RV::at(c, 0 * C::RY + yl)];
-                e1 = s[RV::at(c, 1 * C::RY + yl)];
-            }
-            reinterpret_cast<float4*>(a.out)[gi] = make_float4(e0.x, e0.y, e1.x, e1.y);
+            dif_op_dit<NX, NX, RV, NTHR, 1>(s, twx, tid, XFactors{a.t2.Rx});
+            cluster_exchange<CL, C::RSZ, NTHR>(s, cluster, rank, tid);
+            dif_op_dit<NY, NY, CV, NTHR, 1>(s, twy, tid, YFactors<C::CX, SLO, PB>{a.t2.RyD, a.Nt, unit});
+            plane_move<NX, NY, CL, PB, SLO, NTHR, false, true>(s, nullptr, a.out, rank, unit, NP, tid);
+        } else {
+            plane_move<NX, NY, CL, PB, SLO, NTHR, true, true>(s, nullptr, a.out, rank, unit, NP, tid);
         }
         __syncthreads();
     }
