@@ -8,7 +8,13 @@ than L2, so no flush is needed between passes.  e2e = the same metric through th
 ABI with host buffers: every step uploads the complex128 field from pinned host memory
 (mpc_field_upload), runs the pass (mpc_run_fixed) and downloads it (mpc_field_download).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload W]
+
+--workload picks another cell for its own line (default cell256, the headline above): cell64 is
+the 64x64x512 cell (0.2 mJ, one bench step = one pass of 200 fixed split steps), cell512 the
+512x512x1024 plasma-dominated cell (3 mJ, 120 fs, argon 3 bar) under adaptive step doubling at
+a local-error tolerance of 1e-5 (one bench step = 10 attempts of 3 split steps each; value counts
+the split steps executed, `accepted_pt_steps_per_s` the accepted ones).
 
 --impl reference times the reference's CPU path for this workload -- the FP64 restatement in
 oracle/ (the reference's own FFTW/MPI build cannot be compiled; only plasma.c and a few
@@ -34,7 +40,6 @@ import numpy as np  # noqa: E402
 
 FALLBACK_HBM_GBS = 6800.0
 METRIC = "grid-point-steps/s"
-STEPS_PER_PASS = 400
 BYTES_PER_PT_STEP = 32  # two compulsory complex64 sweeps (read + write) per split step
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 vector rate, nominal
 
@@ -119,9 +124,23 @@ def profile_traffic(name: str):
     return None
 
 
-def make_workload():
+WORKLOADS = {
+    "cell256": dict(config="config2", adaptive=False, per_step=400, cpu_steps=5,
+                    desc="multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
+                    step="one pass of the cell = 400 split steps", profile="pencil_step_256x256x2048.txt"),
+    "cell64": dict(config="config1", adaptive=False, per_step=200, cpu_steps=100,
+                   desc="multipass cell 64x64x512, fixed split steps, lens mirror, SST + ADK + plasma on",
+                   step="one pass of the cell = 200 split steps", profile=None),
+    "cell512": dict(config="config3", adaptive=True, per_step=10, cpu_steps=2,
+                    desc="plasma-dominated cell 512x512x1024 (3 mJ, 120 fs, argon 3 bar), adaptive step "
+                         "doubling at 1e-5, lens mirror, SST + ADK + plasma on",
+                    step="10 step-doubling attempts = 30 split steps", profile=None),
+}
+
+
+def make_workload(name: str = "cell256"):
     from mpc_gb300 import inputs
-    cfg = inputs.config2()
+    cfg = getattr(inputs, WORKLOADS[name]["config"])()
     p, A = inputs.make_cell(cfg)
     return cfg, p, A
 
@@ -156,7 +175,8 @@ def run_reference(args):
         if dist:
             dist.barrier()
         return
-    cfg, p, A = make_workload()
+    wl = WORKLOADS[args.workload]
+    cfg, p, A = make_workload(args.workload)
     cores = os.cpu_count() or 1
     times = []
     for i in range(args.warmup + args.steps):
@@ -169,10 +189,10 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
-            "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
-                       "grid": [p.Nx, p.Ny, p.Nt], "sample": "1 split step per bench step (CPU time bound)"},
+            "config": {"workload": wl["desc"], "grid": [p.Nx, p.Ny, p.Nt],
+                       "sample": "1 split step per bench step (CPU time bound)"},
             "cpu_baseline": {"value": value, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
-                             "sample": "1 split step of the 256x256x2048 cell per bench step, FP64, OpenMP"},
+                             "sample": f"1 split step of the {p.Nx}x{p.Ny}x{p.Nt} cell per bench step, FP64, OpenMP"},
             "e2e": {"value": value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     if dist:
@@ -184,7 +204,8 @@ def run_gb300(args):
     import torch
     torch.cuda.set_device(local)
     from mpc_gb300 import capi
-    cfg, p, A = make_workload()
+    wl = WORKLOADS[args.workload]
+    cfg, p, A = make_workload(args.workload)
     prop = capi.Propagator(p.copy(variant=args.variant))   # -1: the autotuner picks the kernel variant
     vinfo = prop.variant_info()
     # pinned host field for the end-to-end path (physical units, calibrated)
@@ -195,8 +216,14 @@ def run_gb300(args):
     pin.array[:] = prop.download()
     stream = torch.cuda.ExternalStream(prop.stream_handle())
 
+    accepted = [0]
+
     def one_pass():
-        prop.run_fixed(STEPS_PER_PASS)
+        if wl["adaptive"]:
+            for _ in range(wl["per_step"]):
+                accepted[0] += 1 - prop.step_double()["bad"]
+        else:
+            prop.run_fixed(wl["per_step"])
 
     for _ in range(args.warmup):
         one_pass()
@@ -209,6 +236,7 @@ def run_gb300(args):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     launches0 = prop.launch_count()
+    accepted[0] = 0
     ev0.record(stream)
     for _ in range(args.steps):
         one_pass()
@@ -222,8 +250,9 @@ def run_gb300(args):
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    pt_steps = p.N * STEPS_PER_PASS * args.steps
-    value = pt_steps * world / (ms / 1e3)
+    split_steps = (3 if wl["adaptive"] else 1) * wl["per_step"] * args.steps
+    value = p.N * split_steps * world / (ms / 1e3)
+    accepted_rate = p.N * accepted[0] * world / (ms / 1e3)
 
     # per-sweep device time over one extra pass (events around every launch)
     prop.profile(True)
@@ -237,8 +266,9 @@ def run_gb300(args):
     bytes_launch = 16.0 * p.N  # one complex64 read + write of the whole field
     achieved = bytes_launch / (dom_ms / 1e3) / 1e9
     prof_name = {"pencil": "pencil_step_256x256x2048.txt", "plane": "plane_256x256x2048.txt"}[dom]
+    traffic = profile_traffic(prof_name) if wl["profile"] else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": profile_traffic(prof_name), "kernel": f"{dom} sweep",
+                "traffic": traffic, "kernel": f"{dom} sweep",
                 "peak_source": src, "per_sweep_ms": {k: v[0] / max(1, v[1]) for k, v in sweeps.items()},
                 "step_frac_of_32B_floor": (value / world) * BYTES_PER_PT_STEP / (hbm * 1e9)}
 
@@ -250,16 +280,17 @@ def run_gb300(args):
         one_pass()
         prop.download(pin.array)
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": p.N * STEPS_PER_PASS * e2e_steps * world / e2e_s, "unit": "grid-point-steps/s",
+    e2e_split = (3 if wl["adaptive"] else 1) * wl["per_step"] * e2e_steps
+    e2e = {"value": p.N * e2e_split * world / e2e_s, "unit": "grid-point-steps/s",
            "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        nst = 5  # about 10 s on 16 host cores
+        nst = wl["cpu_steps"]  # about 10 s on 16 host cores
         dt = cpu_baseline_run(p, A, nst, cores)
         cpu = {"value": p.N * nst / dt, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{nst} split steps of the 256x256x2048 cell, FP64 oracle/ restatement, OpenMP"}
+               "sample": f"{nst} split steps of the {p.Nx}x{p.Ny}x{p.Nt} cell, FP64 oracle/ restatement, OpenMP"}
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     fp32_peak = nsm * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
     fft_tflops = (value / world) * fft_flop_per_pt_step(p.Nx, p.Ny, p.Nt) / 1e12
@@ -271,12 +302,15 @@ def run_gb300(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
                 "data": "synthetic (seeded Gaussian pulse + 1e-4 noise, argon 1 bar)",
-                "config": {"workload": "multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
-                           "step": "one pass of the cell = 400 split steps", "grid": [p.Nx, p.Ny, p.Nt],
-                           "split_steps_per_step": STEPS_PER_PASS, "l2": "field 1 GiB > L2, no flush",
+                "config": {"workload": wl["desc"], "step": wl["step"], "grid": [p.Nx, p.Ny, p.Nt],
+                           "split_steps_per_step": split_steps // args.steps,
+                           "l2": ("field > L2, no flush" if 8 * p.N > 129e6 else
+                                  "field fits L2: the bench step's passes re-read it from L2"),
                            "parallelism": f"replicas x{world}", "kernel_variant": vinfo},
                 "roofline": roofline, "fft_rate": fft_rate, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clk}
+        if wl["adaptive"]:
+            line["accepted_pt_steps_per_s"] = accepted_rate
         print(json.dumps(line), flush=True)
     prop.close()
     pin.free()
@@ -284,12 +318,12 @@ def run_gb300(args):
         dist.barrier()
 
 
-def run_profile_case(nsteps: int, variant: int = 0):
+def run_profile_case(nsteps: int, variant: int = 0, workload: str = "cell256"):
     """A short target for ncu: upload the workload's field and run `nsteps` split steps,
     with no timing.  Launch order: the entry pencil sweep (template mode 0), then per split
     step one pencil sweep (mode 2) and one plane sweep."""
     from mpc_gb300 import capi
-    cfg, p, A = make_workload()
+    cfg, p, A = make_workload(workload)
     with capi.Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
         prop.run_fixed(nsteps)
@@ -304,6 +338,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="cell256", choices=sorted(WORKLOADS))
     ap.add_argument("--variant", type=int, default=-1,
                     help="kernel variant of the grid (-1: autotune; pin one for profiler runs, whose "
                          "serialised timings mislead the autotuner)")
@@ -311,7 +346,7 @@ def main():
                     help="run NSTEPS split steps of the workload and exit (an ncu target)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case, max(args.variant, 0))
+        run_profile_case(args.profile_case, max(args.variant, 0), args.workload)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -248,8 +248,10 @@ long mpc_launch_count(mpc_ctx *ctx);
 /* The compiled kernel variant this context runs (the autotuner's pick when created with
  * variant = -1) and its launch shapes: info = {P pencils per tile, SLO slots interleaved,
  * CL CTAs per plane cluster, PB planes per cluster unit, PT plane threads per CTA,
- * pencil CTAs launched, plane clusters launched, pencil threads per CTA}. */
-int mpc_variant_info(mpc_ctx *ctx, int *variant, int info[8]);
+ * pencil CTAs launched, plane clusters launched, pencil threads per CTA, LD pencil tile load
+ * mode (0 staged by cp.async, 1 read by the first transform stage), PL plane passes (1 one
+ * cluster kernel, 2 column-strip and row-strip kernels)}. */
+int mpc_variant_info(mpc_ctx *ctx, int *variant, int info[10]);
 /* With on != 0, every pencil and plane sweep is bracketed by CUDA events on the context's
  * stream; mpc_kernel_times sums their durations since the last enable (synchronises). */
 int mpc_profile(mpc_ctx *ctx, int on);

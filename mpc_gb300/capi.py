@@ -319,9 +319,9 @@ class Propagator:
     def variant_info(self) -> dict:
         """The kernel variant this context runs and its launch shapes."""
         v = C.c_int(0)
-        info = (C.c_int * 8)()
+        info = (C.c_int * 10)()
         _check(self.lib.mpc_variant_info(self.h, C.byref(v), info), "mpc_variant_info")
-        keys = ("P", "SLO", "CL", "PB", "PT", "pencil_ctas", "plane_clusters", "pencil_threads")
+        keys = ("P", "SLO", "CL", "PB", "PT", "pencil_ctas", "plane_clusters", "pencil_threads", "LD", "PL")
         return dict(variant=v.value, **dict(zip(keys, list(info))))
 
     def launch_count(self) -> int:

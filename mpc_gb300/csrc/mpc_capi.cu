@@ -563,7 +563,7 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     prof_begin(c, 1, &ev);
     CK(c->ops->plane(a, c->plane_clusters, c->st), "plane kernel launch");
     prof_end(c, 1, ev);
-    c->launches++;
+    c->launches += c->ops->PL == 2 ? 2 + a.lens : 1;
     return MPC_OK;
 }
 
@@ -798,9 +798,9 @@ static int autotune_variant(const mpc_params* p, int* best) {
 int mpc_variant_info(mpc_ctx* c, int* variant, int* info) {
     if (!c || !variant || !info) return fail(MPC_ERR_ARG, "null argument");
     *variant = c->variant;
-    const int v[8] = {c->ops->P, c->ops->SLO, c->ops->CL, c->ops->PB, c->ops->PT, c->pencil_grid,
-                      c->plane_clusters, c->ops->P * c->Nt / c->ops->CH};
-    for (int i = 0; i < 8; i++) info[i] = v[i];
+    const int v[10] = {c->ops->P, c->ops->SLO, c->ops->CL, c->ops->PB, c->ops->PT, c->pencil_grid,
+                       c->plane_clusters, c->ops->P * c->Nt / c->ops->CH, c->ops->LD, c->ops->PL};
+    for (int i = 0; i < 10; i++) info[i] = v[i];
     return MPC_OK;
 }
 

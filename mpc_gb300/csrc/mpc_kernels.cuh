@@ -963,4 +963,132 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_ke
     cluster.sync();
 }
 
+// ---------------------------------------------------------------------------------------
+// Plane pass in two passes over HBM (no clusters), for planes that a cluster of 2-CTA-per-SM
+// blocks cannot hold: the linear step's y part on column strips, then its x part on row strips
+// (IFFT_xy Rx Ry D FFT_xy = (IFFT_x Rx FFT_x)(IFFT_y Ry D FFT_y)).  Slot layout SLO = 1.  Each
+// CTA reads and writes only its own strip, so both passes run in place.
+// ---------------------------------------------------------------------------------------
+// strip of CXS columns of one omega-plane: line = column, position = y
+template <int NY, int CXS>
+struct StripYView {
+    static constexpr int NLINES = CXS;
+    static constexpr __host__ __device__ __forceinline__ int at(int y, int l) { return y * CXS + l; }
+};
+// strip of RYS rows: line = row, position = x, rows padded by one element (bank spread)
+template <int NX, int RYS>
+struct StripXView {
+    static constexpr int NLINES = RYS;
+    static constexpr __host__ __device__ __forceinline__ int at(int x, int l) { return l * (NX + 1) + x; }
+};
+
+template <int NX, int NY, int CXS>
+struct StripYCfg {
+    static constexpr int SIZE = NY * CXS;
+    static constexpr int SMEM = SIZE * 8 + twiddle_bytes(NY);
+    // at least 16 columns: the rows of a warp's butterfly loads then fill all 32 banks
+    static_assert(CXS >= 16 && CXS % 2 == 0 && NX % CXS == 0, "whole float4 column strips");
+};
+template <int NX, int NY, int RYS>
+struct StripXCfg {
+    static constexpr int SIZE = RYS * (NX + 1);
+    static constexpr int SMEM = ((SIZE * 8 + 15) / 16) * 16 + twiddle_bytes(NX);
+    static_assert(NY % RYS == 0 && NX % 2 == 0, "whole row strips");
+};
+
+// Ry(py) D(slot) at strip positions y of any line (the strip is one omega-plane)
+struct YSlotFactors {
+    const float4* __restrict__ RyD;
+    int Nt, slot;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int y0, int) const {
+        const float4* f = RyD + (size_t)y0 * Nt + slot;
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], __ldg(&f[(size_t)q * Nt]));
+    }
+};
+
+// y part: units are (slot, strip of CXS columns); `second` selects the table set t2.
+template <int NX, int NY, int CXS, int NTHR>
+__global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_y_kernel(PlaneArgs a, int second) {
+    using C = StripYCfg<NX, NY, CXS>;
+    using V = StripYView<NY, CXS>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s = reinterpret_cast<float2*>(smem_raw);
+    unsigned char* tw_mem = smem_raw + C::SIZE * 8;
+    const int tid = threadIdx.x;
+    stage_twiddles<NY, NTHR>(tw_mem, a.twy, tid);
+    const Twiddles tw = Twiddles::packed(tw_mem, NY);
+    __syncthreads();
+    const float4* RyD = second ? a.t2.RyD : a.t1.RyD;
+    constexpr int STRIPS = NX / CXS;
+    constexpr int F4_ROW = CXS / 2;
+    const int units = a.Nt * STRIPS;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
+        const float4* g4 = reinterpret_cast<const float4*>(a.in) + ((size_t)slot * a.NP + x0) / 2;
+#pragma unroll 8
+        for (int f = tid; f < NY * F4_ROW; f += NTHR) {
+            const int y = f / F4_ROW, c = f - y * F4_ROW;
+            reinterpret_cast<float4*>(s)[(y * CXS) / 2 + c] = __ldg(&g4[(size_t)y * (NX / 2) + c]);
+        }
+        __syncthreads();
+        dif_op_dit<NY, NY, V, NTHR, 1>(s, tw, tid, YSlotFactors{RyD, a.Nt, slot});
+        float4* o4 = reinterpret_cast<float4*>(a.out) + ((size_t)slot * a.NP + x0) / 2;
+#pragma unroll 8
+        for (int f = tid; f < NY * F4_ROW; f += NTHR) {
+            const int y = f / F4_ROW, c = f - y * F4_ROW;
+            o4[(size_t)y * (NX / 2) + c] = reinterpret_cast<const float4*>(s)[(y * CXS) / 2 + c];
+        }
+        __syncthreads();
+    }
+}
+
+// x part: units are (slot, strip of RYS rows); with the mirror lens, x(t1), the lens, x(t2).
+template <int NX, int NY, int RYS, int NTHR>
+__global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_x_kernel(PlaneArgs a) {
+    using C = StripXCfg<NX, NY, RYS>;
+    using V = StripXView<NX, RYS>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s = reinterpret_cast<float2*>(smem_raw);
+    unsigned char* tw_mem = smem_raw + ((C::SIZE * 8 + 15) / 16) * 16;
+    const int tid = threadIdx.x;
+    stage_twiddles<NX, NTHR>(tw_mem, a.twx, tid);
+    const Twiddles tw = Twiddles::packed(tw_mem, NX);
+    __syncthreads();
+    constexpr int STRIPS = NY / RYS;
+    constexpr int F4_ROW = NX / 2;
+    const int units = a.Nt * STRIPS;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int slot = unit / STRIPS, y0 = (unit - slot * STRIPS) * RYS;
+        const float4* g4 = reinterpret_cast<const float4*>(a.in) + ((size_t)slot * a.NP + (size_t)y0 * NX) / 2;
+#pragma unroll 8
+        for (int f = tid; f < RYS * F4_ROW; f += NTHR) {
+            const int r = f / F4_ROW, c = f - r * F4_ROW;
+            const float4 v = __ldg(&g4[f]);
+            s[V::at(2 * c, r)] = make_float2(v.x, v.y);
+            s[V::at(2 * c + 1, r)] = make_float2(v.z, v.w);
+        }
+        __syncthreads();
+        dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactors{a.t1.Rx});
+        if (a.lens) {
+            for (int e = tid; e < RYS * NX; e += NTHR) {
+                const int x = e % NX, r = e / NX;
+                const int idx = V::at(x, r);
+                s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y0 + r])));
+            }
+            __syncthreads();
+            dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactors{a.t2.Rx});
+        }
+        float4* o4 = reinterpret_cast<float4*>(a.out) + ((size_t)slot * a.NP + (size_t)y0 * NX) / 2;
+#pragma unroll 8
+        for (int f = tid; f < RYS * F4_ROW; f += NTHR) {
+            const int r = f / F4_ROW, c = f - r * F4_ROW;
+            const float2 e0 = s[V::at(2 * c, r)], e1 = s[V::at(2 * c + 1, r)];
+            o4[f] = make_float4(e0.x, e0.y, e1.x, e1.y);
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace mpc

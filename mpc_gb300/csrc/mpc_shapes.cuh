@@ -6,6 +6,10 @@
 //                256-thread CTAs per SM; TP = 16384, CH = 16: one 1024-thread CTA per SM);
 //   SLO          slots interleaved in the layout (default 2 when P = 8, so t-rows are 128 B);
 //   LD           how the split-step pencil pass reads a tile (pencil_kernel);
+//   PL           plane passes: 1, one cluster kernel per sweep (plane_kernel); 2, the y part on
+//                column strips and the x part on row strips, two kernels over HBM without
+//                clusters (plane_y_kernel, plane_x_kernel), for planes larger than a cluster of
+//                two-per-SM CTAs holds;
 //   plane unit   PT threads per CTA and 512 / PT CTAs per SM, each CTA holding a
 //                PLB = 128 KB * PT / 512 share of the unit; SLO == 2: the two interleaved
 //                omega-planes split over CL CTAs; SLO == 1: planes larger than PLB split over
@@ -19,7 +23,7 @@
 namespace mpc {
 
 struct ShapeOps {
-    int Nx, Ny, Nt, P, SLO, CL, PB, PT, CH, LD;
+    int Nx, Ny, Nt, P, SLO, CL, PB, PT, CH, LD, PL;
     int pencil_smem, plane_smem;
     cudaError_t (*setup)();
     cudaError_t (*pencil)(int mode, const PencilArgs&, int grid, cudaStream_t);
@@ -28,14 +32,21 @@ struct ShapeOps {
     int (*pencil_blocks_per_sm)();   // resident split-step pencil CTAs per SM
 };
 
-template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints, int CH = 32, int LD = 1>
+template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints, int CH = 32, int LD = 1,
+          int PL = 1>
 struct Shape {
     static constexpr int P = TP / NT;
     static constexpr int SLO = SLO_ > 0 ? SLO_ : ((P < 16) ? 16 / P : 1);
     static constexpr long PLANE_B = (long)NX * NY * 8;
     static constexpr long PLB = 131072L * PT / kThreads;
-    static constexpr int CL = (SLO == 2) ? (int)(PLANE_B * 2 / PLB) : (PLANE_B > PLB ? (int)(PLANE_B / PLB) : 1);
-    static constexpr int PB = (SLO == 2) ? 2 : (PLANE_B > PLB ? 1 : ((PLB / PLANE_B) < NT ? (int)(PLB / PLANE_B) : NT));
+    static constexpr int CL = PL == 2 ? 1
+                              : (SLO == 2) ? (int)(PLANE_B * 2 / PLB) : (PLANE_B > PLB ? (int)(PLANE_B / PLB) : 1);
+    static constexpr int PB = PL == 2 ? 1
+                              : (SLO == 2) ? 2 : (PLANE_B > PLB ? 1 : ((PLB / PLANE_B) < NT ? (int)(PLB / PLANE_B) : NT));
+    // PL = 2: column strips of CXS columns and row strips of RYS rows, PLB bytes each
+    static constexpr int CXS = (int)(PLB / (NY * 8L)), RYS = (int)(PLB / (NX * 8L));
+    static_assert(PL == 1 || (PL == 2 && SLO == 1 && CXS >= 2 && CXS <= NX && RYS >= 1 && RYS <= NY),
+                  "two-pass planes: SLO 1, strips within the plane");
     static_assert(SLO == 1 || SLO == 2, "slot interleave");
     static_assert(PT == 128 || PT == 256 || PT == 512, "plane threads");
     static_assert(P >= 4 && P <= NX * NY, "pencil tile must fit the grid");
@@ -56,14 +67,31 @@ struct Shape {
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH, LD>), PC::smem(PM_EXIT_C64));
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP, CH, LD>), PC::smem(PM_TEMP));
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ, CH, LD>), PC::smem(PM_IONIZ));
-        MPC_SET_SMEM((plane_kernel<NX, NY, CL, PB, SLO, PT>), LC::SMEM);
-#undef MPC_SET_SMEM
-        if (CL > 8) {
-            e = cudaFuncSetAttribute(plane_kernel<NX, NY, CL, PB, SLO, PT>,
-                                     cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e != cudaSuccess) return e;
+        if constexpr (PL == 2) {
+            MPC_SET_SMEM((plane_y_kernel<NX, NY, CXS, PT>), (StripYCfg<NX, NY, CXS>::SMEM));
+            MPC_SET_SMEM((plane_x_kernel<NX, NY, RYS, PT>), (StripXCfg<NX, NY, RYS>::SMEM));
+            int dev = 0, nsm = 0, by = 0, bx = 0;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, plane_y_kernel<NX, NY, CXS, PT>, PT,
+                                                                   StripYCfg<NX, NY, CXS>::SMEM)) != cudaSuccess)
+                return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, plane_x_kernel<NX, NY, RYS, PT>, PT,
+                                                                   StripXCfg<NX, NY, RYS>::SMEM)) != cudaSuccess)
+                return e;
+            strip_grid_y = by * nsm < NT * (NX / CXS) ? by * nsm : NT * (NX / CXS);
+            strip_grid_x = bx * nsm < NT * (NY / RYS) ? bx * nsm : NT * (NY / RYS);
+            return (by > 0 && bx > 0) ? cudaSuccess : cudaErrorInvalidConfiguration;
+        } else {
+            MPC_SET_SMEM((plane_kernel<NX, NY, CL, PB, SLO, PT>), LC::SMEM);
+            if (CL > 8) {
+                e = cudaFuncSetAttribute(plane_kernel<NX, NY, CL, PB, SLO, PT>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
         }
-        return cudaSuccess;
+#undef MPC_SET_SMEM
     }
 
     static cudaError_t pencil(int mode, const PencilArgs& a, int grid, cudaStream_t st) {
@@ -80,37 +108,53 @@ struct Shape {
         return cudaGetLastError();
     }
 
+    // PL = 2: resident-CTA grids of the two strip kernels (set by setup)
+    static inline int strip_grid_y = 0, strip_grid_x = 0;
+
     static cudaError_t plane(const PlaneArgs& a, int nclusters, cudaStream_t st) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(nclusters * CL);
-        cfg.blockDim = dim3(PT);
-        cfg.dynamicSmemBytes = LC::SMEM;
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = CL;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, plane_kernel<NX, NY, CL, PB, SLO, PT>, a);
+        if constexpr (PL == 2) {
+            PlaneArgs b = a;
+            b.in = a.out;   // the passes after the first run in place
+            plane_y_kernel<NX, NY, CXS, PT><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(a, 0);
+            plane_x_kernel<NX, NY, RYS, PT><<<strip_grid_x, PT, StripXCfg<NX, NY, RYS>::SMEM, st>>>(b);
+            if (a.lens) plane_y_kernel<NX, NY, CXS, PT><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(b, 1);
+            return cudaGetLastError();
+        } else {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(nclusters * CL);
+            cfg.blockDim = dim3(PT);
+            cfg.dynamicSmemBytes = LC::SMEM;
+            cfg.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = CL;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            return cudaLaunchKernelEx(&cfg, plane_kernel<NX, NY, CL, PB, SLO, PT>, a);
+        }
     }
 
     static int max_clusters() {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(CL);
-        cfg.blockDim = dim3(PT);
-        cfg.dynamicSmemBytes = LC::SMEM;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = CL;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, plane_kernel<NX, NY, CL, PB, SLO, PT>, &cfg) != cudaSuccess) return 0;
-        return n;
+        if constexpr (PL == 2) {
+            return strip_grid_y;   // CTAs of the y pass (clusters of one)
+        } else {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(CL);
+            cfg.blockDim = dim3(PT);
+            cfg.dynamicSmemBytes = LC::SMEM;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = CL;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveClusters(&n, plane_kernel<NX, NY, CL, PB, SLO, PT>, &cfg) != cudaSuccess) return 0;
+            return n;
+        }
     }
 
     static int pencil_blocks_per_sm() {
@@ -121,8 +165,13 @@ struct Shape {
         return n;
     }
 
+    static constexpr int plane_smem() {
+        if constexpr (PL == 2) return StripYCfg<NX, NY, CXS>::SMEM;
+        else return LC::SMEM;
+    }
+
     static const ShapeOps* ops() {
-        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PT, CH, LD, PC::SMEM, LC::SMEM, &setup, &pencil, &plane,
+        static const ShapeOps o = {NX, NY, NT, P, SLO, CL, PB, PT, CH, LD, PL, PC::SMEM, plane_smem(), &setup, &pencil, &plane,
                                    &max_clusters, &pencil_blocks_per_sm};
         return &o;
     }

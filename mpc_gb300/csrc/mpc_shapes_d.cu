@@ -1,9 +1,11 @@
-// Kernel instantiations for grid shapes: 512,512,1024 (Nx,Ny,Nt).
+// Kernel instantiations for grid shapes: 512,512,1024 (Nx,Ny,Nt), two variants.
 #include "mpc_shapes.cuh"
 
 namespace mpc {
 extern const ShapeOps* const shape_list_d[];
 const ShapeOps* const shape_list_d[] = {
-    Shape<512,512,1024>::ops(),
+    Shape<512,512,1024,1,256,16384,32,1,2>::ops(),   // plane in two passes: 256-thread CTAs on 16-wide
+                                                     // column and row strips
+    Shape<512,512,1024>::ops(),                      // plane clusters of 16 512-thread CTAs
     nullptr};
 }  // namespace mpc

@@ -251,7 +251,7 @@ int main(int argc, char **argv) {
     st.puls_e = puls_e;
     st.nstep = (chunk > 0) ? (int)llround(z / dzz) : nstep;
     check(mpc_set_state(ctx, &st), "mpc_set_state");
-    int variant_used = 0, info[8];
+    int variant_used = 0, info[10];
     check(mpc_variant_info(ctx, &variant_used, info), "mpc_variant_info");
     printf("Kernel variant %d (pencil tile %d, plane cluster %d x %d threads)\n", variant_used, info[0], info[2], info[4]);
 

@@ -124,14 +124,14 @@ def test_position_frequency_table(N):
 
 
 def _compiled_variants():
-    """(Nx, Ny, Nt, SLO, PT, TP, CH) of every Shape<...>::ops() entry of the shape lists."""
+    """(Nx, Ny, Nt, SLO, PT, TP, CH, LD, PL) of every Shape<...>::ops() entry of the shape lists."""
     import glob
     import re
     out = []
     for f in sorted(glob.glob(os.path.join(ROOT, "mpc_gb300", "csrc", "mpc_shapes_*.cu"))):
         for m in re.finditer(r"Shape<([\d,\s]+)>::ops\(\)", open(f).read()):
             v = [int(x) for x in m.group(1).split(",")]
-            v += [0, 512, 16384, 32][len(v) - 3:]
+            v += [0, 512, 16384, 32, 1, 1][len(v) - 3:]
             out.append(tuple(v))
     return out
 
@@ -139,13 +139,15 @@ def _compiled_variants():
 SHAPES = _compiled_variants()
 
 
-def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32):
+def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32, LD=1, PL=1):
     """Tile and cluster parameters, as mpc_shapes.cuh derives them."""
     P = TP // NT
     SLO = SLO_ if SLO_ > 0 else (16 // P if P < 16 else 1)
     plane_b = NX * NY * 8
     plb = 131072 * PT // 512
-    if SLO == 2:
+    if PL == 2:
+        CL, PB = 1, 1
+    elif SLO == 2:
         CL, PB = plane_b * 2 // plb, 2
     elif plane_b > plb:
         CL, PB = plane_b // plb, 1
@@ -175,11 +177,17 @@ def _views(*variant):
         pl, xl = divmod(l, CX)
         return (y // RY) * RSZ + (pl * RY + (y % RY)) * RS + xl
 
+    if variant[8] == 2:   # two-pass plane: column strips (line = column) and row strips (line = row)
+        plb = 131072 * variant[4] // 512
+        CXS, RYS = plb // (NY * 8), plb // (NX * 8)
+        return [("pencil", NT, P, pen, psize), ("strip_y", NY, CXS, lambda y, l: y * CXS + l, NY * CXS),
+                ("strip_x", NX, RYS, lambda x, l: l * (NX + 1) + x, RYS * (NX + 1))]
     return [("pencil", NT, P, pen, psize), ("row", NX, PB * RY, row, CL * RSZ), ("col", NY, PB * CX, col, CL * RSZ)]
 
 
 def test_variant_list_parsed():
-    assert (256, 256, 2048, 0, 512, 16384, 32) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16) in SHAPES
+    assert (256, 256, 2048, 0, 512, 16384, 32, 1, 1) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16, 1, 1) in SHAPES
+    assert (256, 256, 2048, 1, 256, 8192, 32, 0, 1) in SHAPES and (512, 512, 1024, 1, 256, 16384, 32, 1, 2) in SHAPES
     assert len({v[:3] for v in SHAPES}) >= 7
 
 
@@ -214,6 +222,22 @@ def test_pencil_view_bank_conflict_free(shape):
     for w0 in range(0, min(nthr, 256), 32):
         for i in range(CH):
             assert _wavefronts([at(CH * (t // P) + i, t % P) for t in range(w0, w0 + 32)]) <= 2, (shape, i)
+
+
+@pytest.mark.parametrize("shape", [v for v in SHAPES if v[8] == 2])
+def test_strip_views_bank_conflict_free(shape):
+    """The two-pass plane's strip views: every FFT stage (lines fastest across a warp, as the
+    stage loops take them) reads and writes with the minimum two wavefronts per warp access."""
+    for name, N, NL, at, size in _views(*shape)[1:]:
+        L = N
+        while L > 1:
+            R = 16 if L >= 16 else L
+            S = L // R
+            for w0 in range(0, min(N // R * NL, shape[4]), 32):
+                for q in range(R):
+                    addrs = [at(((idx // NL) // S) * L + (idx // NL) % S + S * q, idx % NL) for idx in range(w0, w0 + 32)]
+                    assert _wavefronts(addrs) <= 2, (shape, name, L, w0, q)
+            L //= R
 
 
 @pytest.mark.parametrize("shape", SHAPES)
