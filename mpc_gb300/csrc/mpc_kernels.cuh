@@ -216,6 +216,7 @@ __device__ __forceinline__ void sincos_small(float x, float* sn, float* cs) {
 // Second-stage probabilities c2 below 2^-60 per slice are flushed to zero: their whole-pencil
 // effect on ions2 is < Nt 2^-60 < 2e-15, far below FP32 resolution, and a tile without any
 // second-stage ionization then skips the (ions2, ions1) scan, which is exact there.
+constexpr float kC2Flush = 8.673617e-19f;   // 2^-60
 struct IonPoint {
     float a, b, c2;  // scan coefficients W1 Kon, Wava Kon, W2 Kon
     float qw;        // sigma w0 tau_c = K4 w0 / (u^2 + w0^2) (defocusing weight)
@@ -244,7 +245,35 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
     r.a = w[0] * c.Kon;
     r.b = r.sigma * I * c.invI1_Kon;
     const float c2 = w[1] * c.Kon;
-    r.c2 = (c2 >= 8.673617e-19f) ? c2 : 0.0f;
+    r.c2 = (c2 >= kC2Flush) ? c2 : 0.0f;
+    return r;
+}
+
+// The first walk of the ionization scan needs only a and b of each sample, and whether any
+// sample of the tile may have a second-stage probability c2 at or above the flush threshold.
+// That is decided on the exponent, e2 > log2(threshold / Kon) - 1, without the second exp2: a
+// conservative test (a tile flagged whose c2 all flush runs the exact (ions2, ions1) scan with
+// zero coefficients).
+struct IonAB {
+    float a, b;
+    bool second;
+};
+__device__ __forceinline__ float ion_second_threshold(const NLConst& c) { return __log2f(kC2Flush / c.Kon) - 1.0f; }
+__device__ __forceinline__ IonAB ion_point_ab(float2 a, const NLConst& c, float e2thr) {
+    IonAB r;
+    float I = fmaf(a.x, a.x, a.y * a.y) * c.I_scale;
+    if (I == 0.0f) I = 1e-30f;                   // plasma.c:136-138
+    const float rs = rsqrtf(I);
+    const float F = I * rs * c.E_c;
+    const float invF = rs * c.inv_E_c;
+    const float l2F = __log2f(F);
+    const float e1 = c.l2K1[0] + c.K5[0] * (c.l2K3[0] - l2F) - c.K3l2e[0] * invF;
+    const float e2 = c.l2K1[1] + c.K5[1] * (c.l2K3[1] - l2F) - c.K3l2e[1] * invF;
+    const float u = c.Kuv * F;
+    const float qw = __fdividef(c.K4w0, fmaf(u, u, c.w0sq));
+    r.a = ((e1 > -126.0f) ? exp2f(e1) : 0.0f) * c.Kon;
+    r.b = qw * u * c.inv_w0 * I * c.invI1_Kon;
+    r.second = e2 > e2thr;
     return r;
 }
 
@@ -273,13 +302,14 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         int any2 = 0;
         {
             float B = 0.0f, C = 0.0f;
+            const float e2thr = ion_second_threshold(c);
 #pragma unroll 8
             for (int i = 0; i < CH; i++) {
-                const IonPoint ip = ion_point(w[V::walk(i)], c);
+                const IonAB ip = ion_point_ab(w[V::walk(i)], c, e2thr);
                 const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
                 C = fmaf(1.0f - ip.b, C, Ck);
                 B = fmaf(-B, ip.b, B + ip.b);
-                any2 |= (ip.c2 > 0.0f);
+                any2 |= ip.second;
             }
             mr[p * TPP + ch] = MapR{(double)B, (double)C};
         }
