@@ -102,10 +102,6 @@ struct PencilArgs {
     NLConst nl;
 };
 
-__device__ __forceinline__ size_t slot_index(int s, int q, int NP, int SLO) {
-    return ((size_t)(s / SLO) * NP + q) * SLO + (s % SLO);
-}
-
 // ---------------------------------------------------------------------------------------
 // Affine-map scans of the ionization prefix (plasma.c:223-231, run forward in t).
 //   R_k = (1 - b_k)(R_{k-1} + a_k) + b_k          map (B, C): R -> (1-B) R + C
@@ -464,10 +460,9 @@ struct PencilCfg {
 // Element order of the two complex values of a float4 row chunk.  For SLO = 2 the pair is
 // (pos 2r, pos 2r + 1) of one pencil; odd rows store them in the opposite order so that
 // the four rows a warp touches fall on both halves of the shared-memory banks.
-// load a slot-layout tile into shared memory, optionally multiplied by -i*omega(pos)
-template <int NT, int P, int SLO, bool DERIV, int TH>
-__device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ g, const float* __restrict__ wpos,
-                                          int q0, int NP, int tid) {
+// load a slot-layout tile into shared memory
+template <int NT, int P, int SLO, int TH>
+__device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ g, int q0, int NP, int tid) {
     using V = PencilView<NT, P>;
     constexpr int F4_PER_ROW = P * SLO / 2;
     constexpr int ROWS = NT / SLO;
@@ -479,12 +474,7 @@ __device__ __forceinline__ void load_tile(float2* s, const float2* __restrict__ 
         int pos0, p0, pos1, p1;
         if constexpr (SLO == 2) { pos0 = 2 * row; pos1 = pos0 + 1; p0 = p1 = c; }
         else { pos0 = pos1 = row; p0 = 2 * c; p1 = p0 + 1; }
-        float2 e0 = make_float2(v.x, v.y), e1 = make_float2(v.z, v.w);
-        if constexpr (DERIV) {
-            const float w0 = __ldg(&wpos[pos0]), w1 = __ldg(&wpos[pos1]);
-            e0 = cscale(mul_mi<false>(e0), w0);
-            e1 = cscale(mul_mi<false>(e1), w1);
-        }
+        const float2 e0 = make_float2(v.x, v.y), e1 = make_float2(v.z, v.w);
         if (SLO == 2 && (row & 1)) {
             s[V::at(pos1, p1)] = e1;
             s[V::at(pos0, p0)] = e0;
@@ -528,7 +518,7 @@ __device__ __forceinline__ void stage_tile(float2* s, const float2* __restrict__
     if constexpr (SLO == 1) {
         load_tile_async<NT, P, TH>(s, g, q0, NP, tid);
     } else {
-        load_tile<NT, P, SLO, false, TH>(s, g, nullptr, q0, NP, tid);
+        load_tile<NT, P, SLO, TH>(s, g, q0, NP, tid);
         __syncthreads();
     }
 }
@@ -677,7 +667,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
             store_tile<NT, P, SLO, TH>(s, reinterpret_cast<float2*>(args.out), q0, NP, tid);
             __syncthreads();
         } else if constexpr (MODE == PM_EXIT_C128 || MODE == PM_EXIT_C64 || MODE == PM_TEMP) {
-            load_tile<NT, P, SLO, false, TH>(s, reinterpret_cast<const float2*>(args.in), args.wpos, q0, NP, tid);
+            load_tile<NT, P, SLO, TH>(s, reinterpret_cast<const float2*>(args.in), q0, NP, tid);
             __syncthreads();
             dit_all<NT, NT, V, TH, kPencilUnroll>(s, tw, tid);
             if constexpr (MODE == PM_TEMP) {

@@ -294,3 +294,53 @@ def test_capi_library_exports_every_header_symbol():
     lib.mpc_shape_supported.argtypes = [C.c_int] * 3
     assert lib.mpc_shape_supported(256, 256, 2048) == 1
     assert lib.mpc_shape_supported(100, 100, 100) == 0
+
+
+def _tw_stage_offset(N, L):
+    """Python statement of tw_stage_offset (mpc_fft.cuh): entries before the stage of sub-length L."""
+    off, M = 0, N
+    while M != L:
+        R = 16 if M >= 16 else M
+        off += M - M // R
+        M //= R
+    return off
+
+
+@pytest.mark.parametrize("N", sorted({v[0] for v in SHAPES} | {v[2] for v in SHAPES}))
+def test_staged_twiddle_layout(N):
+    """The shared-memory twiddle table of a length-N transform in staged order
+    (stage_twiddles): stage L, factor k, butterfly j at tw_stage_offset(N, L) + (k-1) S + j holds
+    W_N^(j k N/L); the stages fill fewer than N entries, each entry once; and a warp's reads of
+    one factor k, lines fastest as the stage loops take them, need at most one wavefront for
+    P >= 4 lines (the natural-order table needed up to 8 at the middle stage of N = 2048)."""
+    seen = {}
+    L = N
+    while L > 1:
+        R = 16 if L >= 16 else L
+        S = L // R
+        off = _tw_stage_offset(N, L)
+        if S > 1:
+            for k in range(1, R):
+                for j in range(S):
+                    i = off + (k - 1) * S + j
+                    assert i not in seen and 0 <= i < N
+                    seen[i] = (j * k * (N // L)) % N
+            for P in (4, 8):
+                for w0 in range(0, N // R * P, 32):
+                    for k in range(1, R):
+                        words = set()
+                        for idx in range(w0, min(w0 + 32, N // R * P)):
+                            j = (idx // P) % S
+                            a = off + (k - 1) * S + j
+                            words |= {2 * a, 2 * a + 1}
+                        per_bank = {}
+                        for w in words:
+                            per_bank.setdefault(w % 32, set()).add(w // 32)
+                        assert max(len(r) for r in per_bank.values()) <= 1, (N, L, P, k)
+        L //= R
+    # the span-1 stage (the last, sub-length L_min <= 16) has no twiddles: the stages before it
+    # fill N - L_min entries (a telescoping sum of L - L/R)
+    L_min = N
+    while L_min > 16:
+        L_min //= 16
+    assert len(seen) == _tw_stage_offset(N, L_min) == N - L_min
