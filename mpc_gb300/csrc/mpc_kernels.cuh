@@ -1,20 +1,20 @@
-// mpc_kernels.cuh -- the split-step propagator's two HBM sweeps and their helpers.
+// mpc_kernels.cuh -- the split-step propagator's sweeps over HBM and their helpers.
 //
 // Device layout of the field between sweeps ("slot layout"): the field is kept in the
 // (x, y, omega) domain, omega in FFT position order.  Slots are interleaved in groups of
 // SLO: element (slot s, pencil q = y*Nx + x) lives at ((s/SLO)*Nx*Ny + q)*SLO + s%SLO.
-// SLO is 2 for Nt = 2048 (8 pencils per tile -> 8*2*8 B = 128 B contiguous per row) and 1
-// for Nt <= 1024 (>= 16 pencils per tile), so every t-row a pencil tile reads is >= 128 B:
-// strided 64 B rows reach only 60% of HBM bandwidth on GB300, 128 B rows 94%.
+// SLO = 2 makes the t-rows of an 8-pencil tile 128 B; the default variants use SLO = 1 (rows of
+// P * 8 B), which keeps every omega-plane contiguous for the plane passes.
 //
 // Sweep 1, pencil pass (one CTA per tile of P neighbouring (x,y) pencils, all of t):
 //   IFFT_t of -i*omega*S -> dA,  IFFT_t of S -> A,  nonlinear step N(dz) (Kerr, self-
 //   steepening, ADK ionization with two affine prefix scans along t, plasma absorption and
 //   defocusing, A *= exp(dz*A_nl)),  FFT_t -> S.
-// Sweep 2, plane pass (one thread-block cluster per unit of omega-planes):
-//   FFT_y, Ry(ky) D(omega) / (Nx Ny Nt), IFFT_y on columns, then FFT_x, Rx(kx), IFFT_x on
-//   rows; the columns become rows in one exchange between the cluster's CTAs through
-//   distributed shared memory.
+// Sweep 2, plane pass, the linear step factorised as (IFFT_x Rx FFT_x)(IFFT_y Ry D FFT_y):
+//   either one kernel per unit of omega-planes on a thread-block cluster (FFT_y, Ry(ky) D(omega)
+//   / (Nx Ny Nt), IFFT_y on columns; the columns become rows in one exchange between the
+//   cluster's CTAs through distributed shared memory; FFT_x, Rx(kx), IFFT_x on rows), or two
+//   kernels without clusters, the y part on column strips and the x part on row strips.
 #pragma once
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>

@@ -1,4 +1,4 @@
-// mpc_shapes.cuh -- per-grid-shape launch configuration of the two sweeps.
+// mpc_shapes.cuh -- per-grid-shape launch configuration of the pencil and plane sweeps.
 //
 // A shape variant fixes the device layout and both sweeps' launch shapes:
 //   pencil tile  P = TP / Nt pencils, P * Nt / CH threads per CTA, one per CH-sample chunk of the
@@ -8,12 +8,12 @@
 //   LD           how the split-step pencil pass reads a tile (pencil_kernel);
 //   PL           plane passes: 1, one cluster kernel per sweep (plane_kernel); 2, the y part on
 //                column strips and the x part on row strips, two kernels over HBM without
-//                clusters (plane_y_kernel, plane_x_kernel), for planes larger than a cluster of
-//                two-per-SM CTAs holds;
+//                clusters (plane_y_kernel, plane_x_kernel), one more pass over HBM but every SM
+//                busy and no cluster barrier (the faster choice on every grid measured);
 //   plane unit   PT threads per CTA and 512 / PT CTAs per SM, each CTA holding a
-//                PLB = 128 KB * PT / 512 share of the unit; SLO == 2: the two interleaved
-//                omega-planes split over CL CTAs; SLO == 1: planes larger than PLB split over
-//                CL CTAs, smaller planes batched PB per CTA.
+//                PLB = 128 KB * PT / 512 share of the unit; PL = 1: SLO == 2, the two interleaved
+//                omega-planes split over CL CTAs; SLO == 1, planes larger than PLB split over
+//                CL CTAs, smaller planes batched PB per CTA; PL = 2: strips of PLB bytes.
 // Several variants of one grid may be compiled in; they differ only in speed.
 #pragma once
 #include <cuda_runtime.h>

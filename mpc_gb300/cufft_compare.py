@@ -4,8 +4,8 @@ A cuFFT implementation of the reference's linear step (propagation.c:3-108) on t
 three library calls: a 3-D complex-to-complex FFT over (t, y, x), one pointwise multiply by
 D(omega) Ry(ky) Rx(kx), and the inverse FFT.  This module times that with cuFFT (through
 torch.fft, complex64, the same 256x256x2048 field) and prints it beside the library's own
-per-launch times of the plane sweep (FFT_x, FFT_y, multiply, inverses in one pass) and the
-pencil sweep (the t transforms fused with the nonlinear step).  cuFFT serves only as the
+per-launch times of the plane sweep (the x and y transforms with their factors) and the pencil
+sweep (the t transforms fused with the nonlinear step).  cuFFT serves only as the
 comparison here; the library never calls it.
 
   python -m mpc_gb300.cufft_compare [--grid 256,256,2048] [--reps 20]
