@@ -197,14 +197,19 @@ def test_create_destroy_leaves_no_pending_error(gpu_lib):
     assert cudart.cudaGetLastError() == 0
 
 
-@pytest.mark.parametrize("grid", [(64, 64, 512), (128, 128, 1024), (256, 256, 512), (256, 256, 2048)])
-def test_kernel_variants_agree(gpu_lib, grid):
+@pytest.mark.parametrize("grid,bounce", [((64, 64, 512), False), ((128, 128, 1024), False), ((256, 256, 512), False),
+                                         ((256, 256, 2048), False), ((128, 128, 1024), True),
+                                         ((256, 256, 512), True), ((256, 256, 2048), True)])
+def test_kernel_variants_agree(gpu_lib, grid, bounce):
     """Every compiled kernel variant of a grid (device layout, tile and launch shapes) gives the
     same field after 6 split steps; an index past the last variant is rejected; the
-    autotuner (variant = -1) picks one of them."""
+    autotuner (variant = -1) picks one of them.  With `bounce`, the cell is 5 steps long at the
+    same step length, so the sixth step crosses the mirror: the plane sweep's lens form
+    (linear step, lens phase, linear step) runs in every variant."""
     from mpc_gb300.capi import MPCError, Propagator
     Nx, Ny, Nt = grid
-    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048)
+    extra = dict(cav=0.5 / 400 * 5, steps_per_pass=5, bounce=BOUNCE_LENS) if bounce else {}
+    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **extra)
     p0, A = inputs.make_cell(cfg)
     ref = None
     v = 0
@@ -221,7 +226,9 @@ def test_kernel_variants_agree(gpu_lib, grid):
         if ref is None:
             ref = out
         else:
-            assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-6, v
+            # same-chunk variants agree bit for bit; 16-sample chunks differ by FP32 composition
+            # (~1e-7 per step), with margin for the stronger field after the lens
+            assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < (2e-6 if bounce else 1e-6), v
         v += 1
     assert v >= 2
     with Propagator(p0.copy(variant=-1)) as prop:
