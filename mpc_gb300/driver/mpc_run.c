@@ -253,7 +253,12 @@ int main(int argc, char **argv) {
     check(mpc_set_state(ctx, &st), "mpc_set_state");
     int variant_used = 0, info[10];
     check(mpc_variant_info(ctx, &variant_used, info), "mpc_variant_info");
-    printf("Kernel variant %d (pencil tile %d, plane cluster %d x %d threads)\n", variant_used, info[0], info[2], info[4]);
+    if (info[9] >= 2)
+        printf("Kernel variant %d (pencil tile %d, plane in two strip passes of %d-thread CTAs)\n", variant_used,
+               info[0], info[4]);
+    else
+        printf("Kernel variant %d (pencil tile %d, plane cluster %d x %d threads)\n", variant_used, info[0], info[2],
+               info[4]);
 
     const long total_fixed = (chunk > 0) ? (long)llround(p.dist / dzz) : 0;
     while (chunk > 0 ? st.nstep < total_fixed : st.z < p.dist) {
