@@ -1028,9 +1028,14 @@ struct YSlotFactors {
     }
 };
 
+// Resident CTAs per SM a strip kernel is compiled for: MINB, or 512 / NTHR (128 registers).
+__host__ __device__ constexpr int strip_min_blocks(int NTHR, int MINB) {
+    return MINB > 0 ? MINB : (NTHR >= 512 ? 1 : 512 / NTHR);
+}
+
 // y part: units are (slot, strip of CXS columns); `second` selects the table set t2.
-template <int NX, int NY, int CXS, int NTHR>
-__global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_y_kernel(PlaneArgs a, int second) {
+template <int NX, int NY, int CXS, int NTHR, int MINB = 0>
+__global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_y_kernel(PlaneArgs a, int second) {
     using C = StripYCfg<NX, NY, CXS>;
     using V = StripYView<NY, CXS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1065,8 +1070,8 @@ __global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_y_
 }
 
 // x part: units are (slot, strip of RYS rows); with the mirror lens, x(t1), the lens, x(t2).
-template <int NX, int NY, int RYS, int NTHR>
-__global__ void __launch_bounds__(NTHR, (NTHR >= 512 ? 1 : 512 / NTHR)) plane_x_kernel(PlaneArgs a) {
+template <int NX, int NY, int RYS, int NTHR, int MINB = 0>
+__global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_x_kernel(PlaneArgs a) {
     using C = StripXCfg<NX, NY, RYS>;
     using V = StripXView<NX, RYS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];

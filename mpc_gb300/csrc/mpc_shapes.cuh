@@ -6,6 +6,8 @@
 //                256-thread CTAs per SM; TP = 16384, CH = 16: one 1024-thread CTA per SM);
 //   SLO          slots interleaved in the layout (default 2 when P = 8, so t-rows are 128 B);
 //   LD           how the split-step pencil pass reads a tile (pencil_kernel);
+//   PMB          PL = 2: resident strip CTAs per SM the strip kernels are compiled for (0: 512 / PT,
+//                at 128 registers; more CTAs hide more load latency at fewer registers each);
 //   PL           plane passes: 1, one cluster kernel per sweep (plane_kernel); 2, the y part on
 //                column strips and the x part on row strips, two kernels over HBM without
 //                clusters (plane_y_kernel, plane_x_kernel), one more pass over HBM but every SM
@@ -33,7 +35,7 @@ struct ShapeOps {
 };
 
 template <int NX, int NY, int NT, int SLO_ = 0, int PT = kThreads, int TP = kTilePoints, int CH = 32, int LD = 1,
-          int PL = 1>
+          int PL = 1, int PMB = 0>
 struct Shape {
     static constexpr int P = TP / NT;
     static constexpr int SLO = SLO_ > 0 ? SLO_ : ((P < 16) ? 16 / P : 1);
@@ -68,15 +70,15 @@ struct Shape {
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP, CH, LD>), PC::smem(PM_TEMP));
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ, CH, LD>), PC::smem(PM_IONIZ));
         if constexpr (PL == 2) {
-            MPC_SET_SMEM((plane_y_kernel<NX, NY, CXS, PT>), (StripYCfg<NX, NY, CXS>::SMEM));
-            MPC_SET_SMEM((plane_x_kernel<NX, NY, RYS, PT>), (StripXCfg<NX, NY, RYS>::SMEM));
+            MPC_SET_SMEM((plane_y_kernel<NX, NY, CXS, PT, PMB>), (StripYCfg<NX, NY, CXS>::SMEM));
+            MPC_SET_SMEM((plane_x_kernel<NX, NY, RYS, PT, PMB>), (StripXCfg<NX, NY, RYS>::SMEM));
             int dev = 0, nsm = 0, by = 0, bx = 0;
             if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
             if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, plane_y_kernel<NX, NY, CXS, PT>, PT,
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, plane_y_kernel<NX, NY, CXS, PT, PMB>, PT,
                                                                    StripYCfg<NX, NY, CXS>::SMEM)) != cudaSuccess)
                 return e;
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, plane_x_kernel<NX, NY, RYS, PT>, PT,
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, plane_x_kernel<NX, NY, RYS, PT, PMB>, PT,
                                                                    StripXCfg<NX, NY, RYS>::SMEM)) != cudaSuccess)
                 return e;
             strip_grid_y = by * nsm < NT * (NX / CXS) ? by * nsm : NT * (NX / CXS);
@@ -115,9 +117,9 @@ struct Shape {
         if constexpr (PL == 2) {
             PlaneArgs b = a;
             b.in = a.out;   // the passes after the first run in place
-            plane_y_kernel<NX, NY, CXS, PT><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(a, 0);
-            plane_x_kernel<NX, NY, RYS, PT><<<strip_grid_x, PT, StripXCfg<NX, NY, RYS>::SMEM, st>>>(b);
-            if (a.lens) plane_y_kernel<NX, NY, CXS, PT><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(b, 1);
+            plane_y_kernel<NX, NY, CXS, PT, PMB><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(a, 0);
+            plane_x_kernel<NX, NY, RYS, PT, PMB><<<strip_grid_x, PT, StripXCfg<NX, NY, RYS>::SMEM, st>>>(b);
+            if (a.lens) plane_y_kernel<NX, NY, CXS, PT, PMB><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(b, 1);
             return cudaGetLastError();
         } else {
             cudaLaunchConfig_t cfg = {};

@@ -1,4 +1,4 @@
-// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt), seven layout / launch
+// Kernel instantiations for grid shapes: 256,256,2048 (Nx,Ny,Nt), eight layout / launch
 // variants (identical results, except 1e-6 relative for the 16-sample chunks; variant 0 is the
 // default, the autotuner times all).
 #include "mpc_shapes.cuh"
@@ -15,5 +15,6 @@ const ShapeOps* const shape_list_c[] = {
     Shape<256,256,2048,1,512>::ops(),              // SLO 1, plane 512 threads, clusters of 4
     Shape<256,256,2048,1,256,16384,16>::ops(),     // SLO 1, 1024-thread pencil CTAs (16-sample chunks)
     Shape<256,256,2048,1,256,8192,32,0,2>::ops(),  // 4-pencil tiles, two-pass plane on 32-wide strips
+    Shape<256,256,2048,1,128,8192,32,0,2,5>::ops(),  // as variant 0, strip kernels at five CTAs per SM
     nullptr};
 }  // namespace mpc

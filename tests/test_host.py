@@ -124,14 +124,14 @@ def test_position_frequency_table(N):
 
 
 def _compiled_variants():
-    """(Nx, Ny, Nt, SLO, PT, TP, CH, LD, PL) of every Shape<...>::ops() entry of the shape lists."""
+    """(Nx, Ny, Nt, SLO, PT, TP, CH, LD, PL, PMB) of every Shape<...>::ops() entry of the shape lists."""
     import glob
     import re
     out = []
     for f in sorted(glob.glob(os.path.join(ROOT, "mpc_gb300", "csrc", "mpc_shapes_*.cu"))):
         for m in re.finditer(r"Shape<([\d,\s]+)>::ops\(\)", open(f).read()):
             v = [int(x) for x in m.group(1).split(",")]
-            v += [0, 512, 16384, 32, 1, 1][len(v) - 3:]
+            v += [0, 512, 16384, 32, 1, 1, 0][len(v) - 3:]
             out.append(tuple(v))
     return out
 
@@ -139,7 +139,7 @@ def _compiled_variants():
 SHAPES = _compiled_variants()
 
 
-def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32, LD=1, PL=1):
+def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32, LD=1, PL=1, PMB=0):
     """Tile and cluster parameters, as mpc_shapes.cuh derives them."""
     P = TP // NT
     SLO = SLO_ if SLO_ > 0 else (16 // P if P < 16 else 1)
@@ -186,8 +186,9 @@ def _views(*variant):
 
 
 def test_variant_list_parsed():
-    assert (256, 256, 2048, 0, 512, 16384, 32, 1, 1) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16, 1, 1) in SHAPES
-    assert (256, 256, 2048, 1, 256, 8192, 32, 0, 1) in SHAPES and (512, 512, 1024, 1, 256, 16384, 32, 1, 2) in SHAPES
+    assert (256, 256, 2048, 0, 512, 16384, 32, 1, 1, 0) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16, 1, 1, 0) in SHAPES
+    assert (256, 256, 2048, 1, 256, 8192, 32, 0, 1, 0) in SHAPES and (512, 512, 1024, 1, 256, 16384, 32, 1, 2, 0) in SHAPES
+    assert (256, 256, 2048, 1, 128, 8192, 32, 0, 2, 5) in SHAPES
     assert len({v[:3] for v in SHAPES}) >= 7
 
 
