@@ -198,8 +198,8 @@ def test_create_destroy_leaves_no_pending_error(gpu_lib):
 
 
 @pytest.mark.parametrize("grid,bounce", [((64, 64, 512), False), ((128, 128, 1024), False), ((256, 256, 512), False),
-                                         ((256, 256, 2048), False), ((128, 128, 1024), True),
-                                         ((256, 256, 512), True), ((256, 256, 2048), True)])
+                                         ((256, 256, 2048), False), ((512, 512, 1024), False),
+                                         ((128, 128, 1024), True), ((256, 256, 512), True), ((256, 256, 2048), True)])
 def test_kernel_variants_agree(gpu_lib, grid, bounce):
     """Every compiled kernel variant of a grid (device layout, tile and launch shapes) gives the
     same field after 6 split steps; an index past the last variant is rejected; the
