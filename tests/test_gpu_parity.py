@@ -235,6 +235,39 @@ def test_kernel_variants_agree(gpu_lib, grid, bounce):
         assert 0 <= prop.variant_info()["variant"] < v
 
 
+@pytest.mark.parametrize("grid", [(128, 128, 1024), (512, 512, 1024)])
+def test_step_double_variants_agree(gpu_lib, grid):
+    """Step-doubling attempts write their trial fields to other buffers than the one they read
+    (the plane sweep out of place); every kernel variant of the grid, cluster or strip plane
+    sweep, gives the same decisions, step sizes and fields (all with 32-sample chunks: the same
+    arithmetic)."""
+    from mpc_gb300.capi import MPCError, Propagator
+    Nx, Ny, Nt = grid
+    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, def_err=1e-5)
+    p0, A = inputs.make_cell(cfg)
+    ref = None
+    v = 0
+    while True:
+        try:
+            prop = Propagator(p0.copy(variant=v))
+        except MPCError:
+            break
+        with prop:
+            prop.upload(A, calibrate=True)
+            rec = [prop.step_double() for _ in range(2)]
+            s = prop.state()
+            out = (rec, s.z, s.dzz, s.nstep, prop.download())
+        if ref is None:
+            ref = out
+        else:
+            assert [r["bad"] for r in out[0]] == [r["bad"] for r in ref[0]], v
+            assert [r["err"] for r in out[0]] == pytest.approx([r["err"] for r in ref[0]], rel=1e-6), v
+            assert out[1:4] == pytest.approx(ref[1:4], rel=1e-12), v
+            assert np.linalg.norm(out[4] - ref[4]) / np.linalg.norm(ref[4]) < 1e-6, v
+        v += 1
+    assert v >= 2
+
+
 @pytest.mark.parametrize("bounce", [BOUNCE_LENS, BOUNCE_SIGNFLIP])
 def test_step_double_matches_oracle(gpu_lib, bounce):
     """Adaptive step-doubling attempts (MPC.c:269-383) on the device field against the
