@@ -8,11 +8,17 @@ per-launch times of the plane sweep (the x and y transforms with their factors) 
 sweep (the t transforms fused with the nonlinear step).  cuFFT serves only as the
 comparison here; the library never calls it.
 
-  python -m mpc_gb300.cufft_compare [--grid 256,256,2048] [--reps 20]
+  python cufft_compare.py [--grid 256,256,2048] [--reps 20]
+
+The plane sweep's time covers its kernels together (two strip passes in the default variant).
 """
 from __future__ import annotations
 
 import json
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 
 def time_cufft_linear(Nx: int, Ny: int, Nt: int, reps: int = 20) -> dict:
@@ -49,8 +55,8 @@ def time_cufft_linear(Nx: int, Ny: int, Nt: int, reps: int = 20) -> dict:
 
 
 def time_library(Nx: int, Ny: int, Nt: int, steps: int = 20, **physics) -> dict:
-    from . import inputs
-    from .capi import Propagator
+    from mpc_gb300 import inputs
+    from mpc_gb300.capi import Propagator
     cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **physics)
     p, A = inputs.make_cell(cfg)
     with Propagator(p.copy(variant=-1)) as prop:

@@ -7,26 +7,37 @@
 #                  declarations of the two kernels it launches under another name;
 #   kernels.cu     with nvcc (its kernels are linked but never launched by the wrapper).
 # The forced-include shims below only add declarations; no reference code is copied.
-# Reads the reference sources (read-only), writes only oracle/_ref/.
+# Reads the reference sources (read-only) from the directory named by MPC_REFERENCE, writes only
+# oracle/_ref/.  Without MPC_REFERENCE, or where it names no reference tree, nothing is built.
 set -euo pipefail
-REF=${MPC_REFERENCE:-/root/reference}
+REF=${MPC_REFERENCE:-}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 CUDA=${CUDA_HOME:-/usr/local/cuda}
 NVCC=${NVCC:-$CUDA/bin/nvcc}
-if [ ! -f "$REF/plasma.c" ]; then
-  echo "reference sources not found at $REF; oracle/_ref not built" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/plasma.c" ]; then
+  echo "reference sources not found (MPC_REFERENCE='$REF'); oracle/_ref not built" >&2
   exit 0
 fi
 mkdir -p "$OUT"
 if [ -f "$OUT/libmpcref.so" ] && [ "$OUT/libmpcref.so" -nt "$HERE/ref_wrap.cpp" ] && [ "$OUT/libmpcref.so" -nt "$0" ]; then
   exit 0
 fi
+# plasma.c's ioniz reads Iion[2] of a two-element block (plasma.c:153,163).  The shim gives every
+# allocation of plasma.c a zeroed tail and puts the value ref_ioniz states (mpcref_iion2) in
+# slot 2 of each two-double block, so that the read is defined and the same on every host.
 cat > "$OUT/shim_host.h" <<'EOF'
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
+extern "C" double mpcref_iion2;
+static inline void* mpcref_malloc(size_t n) {
+    double* p = (double*)calloc(1, n + 4 * sizeof(double));
+    if (p && n == 2 * sizeof(double)) p[2] = mpcref_iion2;
+    return p;
+}
+#define malloc(n) mpcref_malloc(n)
 EOF
 cat > "$OUT/shim_cu.h" <<'EOF'
 #include <cstdio>

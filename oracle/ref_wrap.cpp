@@ -22,21 +22,20 @@ void ref_ADK(long n, double* r1, double* r2, double* C_nl, double* f_lm, double*
     ADK(r1, r2, dims, C_nl, f_lm, nq, mq, Ei, E);
 }
 
-// ioniz reads Iion[2] from a two-element heap block (plasma.c:276).  That value only feeds
-// the second-stage rate W2, which the as-written descending scan multiplies by zero; to keep
-// the run deterministic the 32-byte heap chunk that ioniz's malloc(2*sizeof(double)) will
-// reuse (glibc's per-thread cache returns the most recently freed chunk of that size) is
-// primed so that index 2 holds `iion2` (the second ionization potential in Hartree).
+// ioniz reads Iion[2] from a two-element heap block (plasma.c:163).  That value only feeds
+// the second-stage rate W2, which the as-written descending scan multiplies by zero.  plasma.c is
+// compiled with an allocation shim (oracle/build_ref.sh) that places mpcref_iion2 in slot 2 of
+// every two-double block, so the run is defined: ref_ioniz sets it to `iion2` (the second
+// ionization potential in Hartree).
+extern "C" double mpcref_iion2;
+double mpcref_iion2 = 0.0;
 void ref_ioniz(double* A, int Nx, int Ny, int Nt, double w0, double deltat, const char* gas, double rho_c,
                double* w, double rho_nt, double n0, double* tau_c, double* fe, double iion2) {
     int dims[3] = {Nx, Ny, Nt};
     char g[16];
     strncpy(g, gas, sizeof g - 1);
     g[sizeof g - 1] = 0;
-    double* prime = (double*)malloc(3 * sizeof(double));
-    prime[0] = prime[1] = 0.0;
-    prime[2] = iion2;
-    free(prime);
+    mpcref_iion2 = iion2;
     ioniz(reinterpret_cast<cufftDoubleComplex*>(A), dims, w0, deltat, g, rho_c, w, rho_nt, n0, tau_c, fe);
 }
 

@@ -113,3 +113,13 @@ def test_vectors_reproduce_from_reference():
     a = C.c_double(0); b = C.c_double(0)
     lib.ref_ionizpot(b"Argon", C.byref(a), C.byref(b))
     assert a.value == G["gas_I1"][0]
+    # ioniz as written, on the stored pulse
+    Nx, Ny, Nt = (int(v) for v in G["ioniz_dims"])
+    w0, dt, rho_c, rho_nt, n0 = (float(v) for v in G["ioniz_scalars"])
+    A = np.ascontiguousarray(G["ioniz_A"])
+    w = np.ascontiguousarray(G["ioniz_w"])
+    tau = np.zeros(A.size); fe = np.zeros(A.size)
+    lib.ref_ioniz(make_golden._p(A.view(np.float64)), Nx, Ny, Nt, w0, dt, b"Argon", rho_c, make_golden._p(w), rho_nt,
+                  n0, make_golden._p(tau), make_golden._p(fe), float(G["adk_Iion"][1]))
+    np.testing.assert_array_equal(tau, G["ioniz_tau"])
+    np.testing.assert_array_equal(fe, G["ioniz_fe"])
