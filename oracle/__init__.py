@@ -1,9 +1,12 @@
-"""ctypes wrapper of the FP64 CPU oracle (oracle/mpc_oracle.c).
+"""ctypes wrappers of the FP64 oracles: the CPU restatement (oracle/mpc_oracle.c) and its
+FP64 GPU counterpart (oracle/mpc_oracle64.cu, cuFFT Z2Z plus FP64 kernels) for whole runs of the
+large cells.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by bench.py's
 cpu_baseline / reference arm, as the checker and the CPU baseline.  The product package
 never imports it.  build() compiles liboracle.so with gcc (OpenMP, -ffp-contract=off so
-x86 and Arm hosts round alike).
+x86 and Arm hosts round alike) and liboracle64.so with nvcc (--fmad=false, linked against
+liboracle.so for the phase tables, the beam-size search and the step rule).
 """
 from __future__ import annotations
 
@@ -18,6 +21,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SRC = os.path.join(HERE, "mpc_oracle.c")
 HDR = os.path.join(HERE, "mpc_oracle.h")
+LIB64 = os.path.join(BUILD, "liboracle64.so")
+SRC64 = os.path.join(HERE, "mpc_oracle64.cu")
+HDR64 = os.path.join(HERE, "mpc_oracle64.h")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -55,6 +61,27 @@ def build(force: bool = False) -> str:
            "-o", LIB, SRC, "-lm"]
     subprocess.run(cmd, check=True)
     return LIB
+
+
+def _nvcc() -> str:
+    import shutil
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def build64(force: bool = False) -> str:
+    """liboracle64.so: the FP64 GPU oracle for sm_103a, linked against liboracle.so."""
+    build(force)
+    deps = [SRC64, HDR64, HDR, LIB]
+    if not force and os.path.exists(LIB64) and os.path.getmtime(LIB64) >= max(os.path.getmtime(d) for d in deps):
+        return LIB64
+    cmd = [_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "--fmad=false",
+           "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared", "-o", LIB64, SRC64, f"-L{BUILD}", "-l:liboracle.so",
+           "-Xlinker", "-rpath,$ORIGIN", "-lcufft"]
+    subprocess.run(cmd, check=True)
+    return LIB64
 
 
 _lib = None
@@ -250,3 +277,96 @@ def setStep(dzz: float, C1: np.ndarray, C2: np.ndarray, def_err: float, dzmin: f
     lib().or_setStep(C1.size, C.byref(d), _p(C1.view(np.float64)), _p(C2.view(np.float64)), def_err, dzmin, _p(y1), _p(y2),
                      C.byref(bad), C.byref(err))
     return d.value, bad.value, err.value
+
+
+# ---- FP64 GPU oracle -------------------------------------------------------------------
+_lib64 = None
+
+
+def lib64() -> C.CDLL:
+    global _lib64
+    if _lib64 is None:
+        _lib64 = C.CDLL(build64())
+        L = _lib64
+        cd = C.POINTER(C.c_double)
+        L.or64_last_error.restype = C.c_char_p
+        L.or64_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(or_params), C.POINTER(or_switches)]
+        L.or64_destroy.argtypes = [C.c_void_p]
+        L.or64_upload.argtypes = [C.c_void_p, cd]
+        L.or64_download.argtypes = [C.c_void_p, cd]
+        L.or64_ssfmprop.argtypes = [C.c_void_p, C.c_double, _ip, C.c_double, cd, cd, cd, cd, cd, cd, cd, C.c_int]
+        L.or64_run_fixed.argtypes = [C.c_void_p, C.POINTER(or_state), C.c_int]
+        L.or64_double_step.argtypes = [C.c_void_p, C.POINTER(or_state), C.c_double, C.c_int, _ip, cd]
+        L.or64_energy.argtypes = [C.c_void_p, cd]
+    return _lib64
+
+
+class Oracle64(Oracle):
+    """The FP64 GPU oracle on the current CUDA device, holding the field (complex128) there.
+    Same parameter record and switches as Oracle; the field stays on the device between calls."""
+
+    def __init__(self, p, **sw):
+        super().__init__(p, **sw)
+        self.L64 = lib64()
+        self.ctx = C.c_void_p()
+        if self.L64.or64_create(C.byref(self.ctx), C.byref(self.op), C.byref(self.sw)) != 0:
+            raise RuntimeError(f"or64_create: {self.L64.or64_last_error().decode()}")
+
+    def _ck(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise RuntimeError(f"{what}: {self.L64.or64_last_error().decode()}")
+
+    def close(self) -> None:
+        if self.ctx:
+            self.L64.or64_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, A: np.ndarray) -> None:
+        A = np.ascontiguousarray(A, dtype=np.complex128)
+        self._ck(self.L64.or64_upload(self.ctx, _p(A.view(np.float64))), "upload")
+
+    def download(self) -> np.ndarray:
+        out = np.empty(int(np.prod(self.p.dims)), dtype=np.complex128)
+        self._ck(self.L64.or64_download(self.ctx, _p(out.view(np.float64))), "download")
+        return out
+
+    def ssfmprop_dev(self, dzz: float, signmem: int, z: float, puls_e: float, change: int = 0):
+        sm = C.c_int(signmem)
+        pe = C.c_double(puls_e)
+        BP1 = np.zeros(self.p.dims[0])
+        BP2 = np.zeros(self.p.dims[1])
+        y1 = np.zeros(4)
+        y2 = np.zeros(4)
+        b1 = C.c_double(0)
+        b2 = C.c_double(0)
+        self._ck(self.L64.or64_ssfmprop(self.ctx, dzz, C.byref(sm), z, C.byref(pe), _p(BP1), _p(BP2), _p(y1), _p(y2),
+                                        C.byref(b1), C.byref(b2), change), "ssfmprop")
+        return dict(signmem=sm.value, puls_e=pe.value, BP1=BP1, BP2=BP2, y1=y1, y2=y2, bps1=b1.value, bps2=b2.value)
+
+    def run_fixed_dev(self, st: or_state, nsteps: int) -> None:
+        self._ck(self.L64.or64_run_fixed(self.ctx, C.byref(st), nsteps), "run_fixed")
+
+    def double_step_dev(self, st: or_state, dz_used: float = 0.0, force: int = -1):
+        """One attempt on the resident field; returns (own_bad, own_err) of this oracle's rule."""
+        ob = C.c_int(0)
+        oe = C.c_double(0)
+        self._ck(self.L64.or64_double_step(self.ctx, C.byref(st), dz_used, force, C.byref(ob), C.byref(oe)),
+                 "double_step")
+        return ob.value, oe.value
+
+    def energy_dev(self) -> float:
+        e = C.c_double(0)
+        self._ck(self.L64.or64_energy(self.ctx, C.byref(e)), "energy")
+        return e.value

@@ -65,7 +65,7 @@ void or_set_threads(int n) {
  * ---------------------------------------------------------------------------------- */
 #define BLK 8
 
-static void make_twiddles(int n, double complex *tw, int *rev) {
+static void make_twiddles(int n, or_complex *tw, int *rev) {
     for (int j = 0; j < n / 2; j++) {
         double a = -2.0 * M_PI * (double)j / (double)n;
         tw[j] = cos(a) + I * sin(a);
@@ -81,8 +81,8 @@ static void make_twiddles(int n, double complex *tw, int *rev) {
 }
 
 /* transform nb (<= BLK) lines whose element i sits at base[b] + i*stride */
-static void fft_block(double complex *const *base, int nb, long stride, int n, int sign,
-                      const double complex *tw, const int *rev, double complex *buf) {
+static void fft_block(or_complex *const *base, int nb, long stride, int n, int sign,
+                      const or_complex *tw, const int *rev, or_complex *buf) {
     for (int i = 0; i < n; i++) {
         const long src = (long)rev[i] * stride;
         for (int b = 0; b < nb; b++) buf[(long)i * BLK + b] = base[b][src];
@@ -92,12 +92,12 @@ static void fft_block(double complex *const *base, int nb, long stride, int n, i
         const int half = len >> 1, step = n / len;
         for (int s = 0; s < n; s += len) {
             for (int j = 0; j < half; j++) {
-                double complex wj = tw[j * step];
+                or_complex wj = tw[j * step];
                 if (sign > 0) wj = conj(wj);
-                double complex *u = buf + (long)(s + j) * BLK;
-                double complex *v = buf + (long)(s + j + half) * BLK;
+                or_complex *u = buf + (long)(s + j) * BLK;
+                or_complex *v = buf + (long)(s + j + half) * BLK;
                 for (int b = 0; b < BLK; b++) {
-                    const double complex t = v[b] * wj;
+                    const or_complex t = v[b] * wj;
                     v[b] = u[b] - t;
                     u[b] = u[b] + t;
                 }
@@ -111,21 +111,21 @@ static void fft_block(double complex *const *base, int nb, long stride, int n, i
 }
 
 /* Batched strided FFTs with the strides of the FFTW guru plans, propagation.c:563-603. */
-void or_fft_axis(double complex *A, int Nx, int Ny, int Nt, int axis, int sign) {
+void or_fft_axis(or_complex *A, int Nx, int Ny, int Nt, int axis, int sign) {
     int n;
     long stride, nlines;
     if (axis == 0) { n = Nx; stride = 1; nlines = (long)Ny * Nt; }
     else if (axis == 1) { n = Ny; stride = Nx; nlines = (long)Nx * Nt; }
     else { n = Nt; stride = (long)Nx * Ny; nlines = (long)Nx * Ny; }
     if (n <= 1) return;
-    double complex *tw = (double complex *)malloc(sizeof(double complex) * (n / 2 + 1));
+    or_complex *tw = (or_complex *)malloc(sizeof(or_complex) * (n / 2 + 1));
     int *rev = (int *)malloc(sizeof(int) * n);
     make_twiddles(n, tw, rev);
     const long nblk = (nlines + BLK - 1) / BLK;
 #pragma omp parallel
     {
-        double complex *buf = (double complex *)malloc(sizeof(double complex) * (long)n * BLK);
-        double complex *base[BLK];
+        or_complex *buf = (or_complex *)malloc(sizeof(or_complex) * (long)n * BLK);
+        or_complex *base[BLK];
 #pragma omp for schedule(static)
         for (long bl = 0; bl < nblk; bl++) {
             int nb = 0;
@@ -148,8 +148,8 @@ void or_fft_axis(double complex *A, int Nx, int Ny, int Nt, int axis, int sign) 
 
 /* kernels.cu:47-54 (calcexpD0CUDA) / propagation.c:150-153, then fftshift axis 0
  * (propagation.c:393-402): swap the two halves. */
-void or_expD0(double complex *out, int Nt, double dzz, double alpha, const double *betas) {
-    double complex *tmp = (double complex *)malloc(sizeof(double complex) * Nt);
+void or_expD0(or_complex *out, int Nt, double dzz, double alpha, const double *betas) {
+    or_complex *tmp = (or_complex *)malloc(sizeof(or_complex) * Nt);
     for (int k = 0; k < Nt; k++) tmp[k] = cexp(dzz / 2.0 * (I * betas[k] - alpha / 2.0));
     for (int k = 0; k < Nt / 2; k++) {
         out[k] = tmp[Nt / 2 + k];
@@ -166,7 +166,7 @@ static int pass_sign(double z, double Cav) {
 /* propagation.c:375-391.  As written the exponent is real (the i of the commented line
  * 389 is dropped, A12), the table stays in centred order while the linear step indexes
  * it in FFT order (A12), and the centre is the mean of the two middle entries (A23). */
-void or_calcexpR(double complex *expR, int n, int nwr, int *signmem, double z, double Cav,
+void or_calcexpR(or_complex *expR, int n, int nwr, int *signmem, double z, double Cav,
                  double k0, double dzh, const double *wr, const or_switches *sw) {
     int signum = pass_sign(z, Cav);
     if (-*signmem == signum) *signmem = -*signmem;
@@ -183,8 +183,8 @@ void or_calcexpR(double complex *expR, int n, int nwr, int *signmem, double z, d
 }
 
 /* propagation.c:65-108 (FFTW branch; A9: the index is j*Nx + i). */
-void or_linearstep(double complex *A, int Nx, int Ny, int Nt, const double complex *expD0,
-                   const double complex *expRx, const double complex *expRy) {
+void or_linearstep(or_complex *A, int Nx, int Ny, int Nt, const or_complex *expD0,
+                   const or_complex *expRx, const or_complex *expRy) {
     const long NP = (long)Nx * Ny, N = NP * Nt;
     or_fft_axis(A, Nx, Ny, Nt, 2, -1);
 #pragma omp parallel for schedule(static)
@@ -209,8 +209,8 @@ void or_linearstep(double complex *A, int Nx, int Ny, int Nt, const double compl
 }
 
 /* propagation.c:164-177 (wbuff = fftshift(w)) and 215-233 (FFTW branch of the SST). */
-void or_sst(const double complex *A, int Nx, int Ny, int Nt, const double *w, double gamma2,
-            double w0, double complex *sst) {
+void or_sst(const or_complex *A, int Nx, int Ny, int Nt, const double *w, double gamma2,
+            double w0, or_complex *sst) {
     const long NP = (long)Nx * Ny, N = NP * Nt;
     double *wbuff = (double *)malloc(sizeof(double) * Nt);
     memcpy(wbuff, w, sizeof(double) * Nt);
@@ -218,8 +218,8 @@ void or_sst(const double complex *A, int Nx, int Ny, int Nt, const double *w, do
         wbuff[k] = w[Nt / 2 + k];
         wbuff[Nt / 2 + k] = w[k];
     }
-    double complex *dA = (double complex *)malloc(sizeof(double complex) * N);
-    memcpy(dA, A, sizeof(double complex) * N);
+    or_complex *dA = (or_complex *)malloc(sizeof(or_complex) * N);
+    memcpy(dA, A, sizeof(or_complex) * N);
     or_fft_axis(dA, Nx, Ny, Nt, 2, -1);
 #pragma omp parallel for schedule(static)
     for (long k = 0; k < Nt; k++)
@@ -227,7 +227,7 @@ void or_sst(const double complex *A, int Nx, int Ny, int Nt, const double *w, do
     or_fft_axis(dA, Nx, Ny, Nt, 2, +1);
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < N; q++) {
-        const double complex d = dA[q] / (double)Nt;
+        const or_complex d = dA[q] / (double)Nt;
         sst[q] = gamma2 / w0 * (2.0 * d * conj(A[q]) + A[q] * conj(d));
     }
     free(dA);
@@ -304,7 +304,7 @@ static void adk_consts(const char *gas, const or_switches *sw, double *I1, doubl
 
 /* plasma.c:118-245, one (x,y) pencil at a time.  The per-point arithmetic is that of the
  * reference's whole-field loops; only the storage is per pencil. */
-void or_ioniz(const double complex *A, int Nx, int Ny, int Nt, double w0, double deltat,
+void or_ioniz(const or_complex *A, int Nx, int Ny, int Nt, double w0, double deltat,
               const char *gas, double rho_c, const double *w, double rho_nt, double n0,
               double *tau_c, double *fe_sp, const or_switches *sw) {
     const long NP = (long)Nx * Ny;
@@ -401,7 +401,7 @@ void or_calc1oes(const double *BP, int n, const double *r, double *vald1oes, dou
     y[3] = BP[posi2];
 }
 
-void or_beam_profiles(const double complex *A, int Nx, int Ny, int Nt, double *BP1, double *BP2) {
+void or_beam_profiles(const or_complex *A, int Nx, int Ny, int Nt, double *BP1, double *BP2) {
     const long NP = (long)Nx * Ny;
     memset(BP1, 0, sizeof(double) * Nx);
     memset(BP2, 0, sizeof(double) * Ny);
@@ -415,23 +415,23 @@ void or_beam_profiles(const double complex *A, int Nx, int Ny, int Nt, double *B
 }
 
 /* propagation.c:111-372 */
-void or_ssfmprop(double complex *A, const or_params *p, double dzz, int *signmem, double z,
+void or_ssfmprop(or_complex *A, const or_params *p, double dzz, int *signmem, double z,
                  double *puls_e, double *BP1, double *BP2, double *y1, double *y2,
                  double *bps1, double *bps2, int change, const or_switches *sw) {
     const int Nx = p->Nx, Ny = p->Ny, Nt = p->Nt;
     const long NP = (long)Nx * Ny, N = NP * Nt;
-    double complex *expD0 = (double complex *)malloc(sizeof(double complex) * Nt);
-    double complex *expRx = (double complex *)malloc(sizeof(double complex) * Nx);
-    double complex *expRy = (double complex *)malloc(sizeof(double complex) * Ny);
+    or_complex *expD0 = (or_complex *)malloc(sizeof(or_complex) * Nt);
+    or_complex *expRx = (or_complex *)malloc(sizeof(or_complex) * Nx);
+    or_complex *expRy = (or_complex *)malloc(sizeof(or_complex) * Ny);
     or_expD0(expD0, Nt, dzz, p->alpha, p->betas);
     or_calcexpR(expRx, Nx, Ny, signmem, z, p->Cav, p->k0, dzz / 2, p->wr, sw);
     or_calcexpR(expRy, Ny, Ny, signmem, z, p->Cav, p->k0, dzz / 2, p->wr, sw);
     or_linearstep(A, Nx, Ny, Nt, expD0, expRx, expRy);
 
-    double complex *buffer = (double complex *)calloc(N, sizeof(double complex));
+    or_complex *buffer = (or_complex *)calloc(N, sizeof(or_complex));
     if (p->sst_on == 1) or_sst(A, Nx, Ny, Nt, p->w, p->gamma2, p->w0, buffer);
 
-    double complex *A_nl = (double complex *)malloc(sizeof(double complex) * N);
+    or_complex *A_nl = (or_complex *)malloc(sizeof(or_complex) * N);
     if (p->plasm == 1) {
         double *tau_c = (double *)malloc(sizeof(double) * N);
         double *fe = (double *)malloc(sizeof(double) * N);
@@ -491,30 +491,23 @@ void or_ssfmprop(double complex *A, const or_params *p, double dzz, int *signmem
     free(expRy);
 }
 
-/* propagation.c:616-677 (printing dropped). */
-void or_setStep(long n, double *dzz, const double complex *C1, const double complex *C2,
-                double def_err, double dzmin, const double *y1, const double *y2, int *bad,
-                double *err) {
-    double sum1 = 0, sum2 = 0, ujdz;
+/* propagation.c:636-676: the dz update for a local error err. */
+void or_step_rule(double err, double *dzz, double def_err, double dzmin, const double *y1,
+                  const double *y2, int *bad) {
+    double ujdz;
     *bad = 0;
-    for (long i = 0; i < n; i++) {
-        const double complex CC = C2[i] - C1[i];
-        sum1 += pow(cabs(CC), 2);
-        sum2 += pow(cabs(C2[i]), 2);
-    }
-    *err = sqrt(sum1) / sqrt(sum2);
     const double err_fact = pow(2.0, (1.0 / 3.0));
-    if (*err > 2.0 * def_err) {
+    if (err > 2.0 * def_err) {
         ujdz = *dzz / 2.0;
         if (ujdz > dzmin) {
             *dzz = ujdz;
             *bad = 1;
             return;
         }
-    } else if (*err > def_err && *err < 2.0 * def_err) {
+    } else if (err > def_err && err < 2.0 * def_err) {
         ujdz = *dzz / err_fact;
         if (ujdz > dzmin) *dzz = ujdz;
-    } else if (*err > 0.5 * def_err && *err <= def_err) {
+    } else if (err > 0.5 * def_err && err <= def_err) {
         /* keep */
     } else {
         ujdz = *dzz * err_fact;
@@ -522,24 +515,38 @@ void or_setStep(long n, double *dzz, const double complex *C1, const double comp
     }
 }
 
+/* propagation.c:616-677 (printing dropped): the error sums (:624-633), then the rule. */
+void or_setStep(long n, double *dzz, const or_complex *C1, const or_complex *C2,
+                double def_err, double dzmin, const double *y1, const double *y2, int *bad,
+                double *err) {
+    double sum1 = 0, sum2 = 0;
+    for (long i = 0; i < n; i++) {
+        const or_complex CC = C2[i] - C1[i];
+        sum1 += pow(cabs(CC), 2);
+        sum2 += pow(cabs(C2[i]), 2);
+    }
+    *err = sqrt(sum1) / sqrt(sum2);
+    or_step_rule(*err, dzz, def_err, dzmin, y1, y2, bad);
+}
+
 /* MPC.c:389-449 (GPU branch: intensity sums; the spectrum stays in FFT order). */
-void or_diag(const double complex *A, int Nx, int Ny, int Nt, double *temp, double *spec) {
+void or_diag(const or_complex *A, int Nx, int Ny, int Nt, double *temp, double *spec) {
     const long NP = (long)Nx * Ny, N = NP * Nt;
     for (long k = 0; k < Nt; k++) {
         double s = 0;
         for (long i = 0; i < NP; i++) {
-            const double complex a = A[k * NP + i];
+            const or_complex a = A[k * NP + i];
             s += creal(a) * creal(a) + cimag(a) * cimag(a);
         }
         temp[k] = s;
     }
-    double complex *C = (double complex *)malloc(sizeof(double complex) * N);
-    memcpy(C, A, sizeof(double complex) * N);
+    or_complex *C = (or_complex *)malloc(sizeof(or_complex) * N);
+    memcpy(C, A, sizeof(or_complex) * N);
     or_fft_axis(C, Nx, Ny, Nt, 2, -1);
     for (long k = 0; k < Nt; k++) {
         double s = 0;
         for (long i = 0; i < NP; i++) {
-            const double complex a = C[k * NP + i];
+            const or_complex a = C[k * NP + i];
             s += creal(a) * creal(a) + cimag(a) * cimag(a);
         }
         spec[k] = s;
@@ -548,7 +555,7 @@ void or_diag(const double complex *A, int Nx, int Ny, int Nt, double *temp, doub
 }
 
 /* MPC.c:206-216 (A17: both parts scaled) */
-void or_calibrate(double complex *A, long n, double puls_e, double Esig, const or_switches *sw) {
+void or_calibrate(or_complex *A, long n, double puls_e, double Esig, const or_switches *sw) {
     const double Ksn = sqrt(puls_e / Esig);
     for (long i = 0; i < n; i++) {
         if (sw->energy_both) A[i] *= Ksn;
@@ -556,7 +563,7 @@ void or_calibrate(double complex *A, long n, double puls_e, double Esig, const o
     }
 }
 
-void or_mirror_lens(double complex *A, int Nx, int Ny, int Nt, const double *r, double k0,
+void or_mirror_lens(or_complex *A, int Nx, int Ny, int Nt, const double *r, double k0,
                     double roc) {
     const long NP = (long)Nx * Ny;
 #pragma omp parallel for schedule(static)
@@ -574,7 +581,7 @@ static int bounces_between(double z0, double z1, double Cav) {
     return (int)(floor(z1 / Cav + eps) - floor(z0 / Cav + eps));
 }
 
-void or_run_fixed(double complex *A, const or_params *p, or_state *st, int nsteps,
+void or_run_fixed(or_complex *A, const or_params *p, or_state *st, int nsteps,
                   const or_switches *sw) {
     for (int s = 0; s < nsteps; s++) {
         /* the pass index is taken from the step count so that z = s*dz lands on the
@@ -595,13 +602,13 @@ void or_run_fixed(double complex *A, const or_params *p, or_state *st, int nstep
     }
 }
 
-void or_double_step(double complex *A, double complex *C1, double complex *C2,
+void or_double_step(or_complex *A, or_complex *C1, or_complex *C2,
                     const or_params *p, or_state *st, const or_switches *sw) {
     const long N = (long)p->Nx * p->Ny * p->Nt;
     double *BP1 = (double *)malloc(sizeof(double) * p->Nx);
     double *BP2 = (double *)malloc(sizeof(double) * p->Ny);
-    memcpy(C1, A, sizeof(double complex) * N);
-    memcpy(C2, A, sizeof(double complex) * N);
+    memcpy(C1, A, sizeof(or_complex) * N);
+    memcpy(C2, A, sizeof(or_complex) * N);
     const double dz_used = st->dzz;
     or_ssfmprop(C1, p, 2 * dz_used, &st->signmem, st->z, &st->puls_e, BP1, BP2, st->y1, st->y2,
                 &st->bps1, &st->bps2, 0, sw);

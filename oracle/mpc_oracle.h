@@ -19,10 +19,15 @@
  */
 #ifndef MPC_ORACLE_H
 #define MPC_ORACLE_H
-#include <complex.h>
-
+/* C99 double complex in C; the layout-identical std::complex<double> when the header is
+ * included from C++ (the FP64 GPU oracle, mpc_oracle64.cu) */
 #ifdef __cplusplus
+#include <complex>
+typedef std::complex<double> or_complex;
 extern "C" {
+#else
+#include <complex.h>
+typedef double complex or_complex;
 #endif
 
 /* Run parameters in the order of param.bin (MPC.c:77,180-203) plus the mirror
@@ -67,31 +72,31 @@ void or_set_threads(int n);
 
 /* Unnormalised strided 1-D FFTs along one axis of the 3-D field.
  * axis 0 = x, 1 = y, 2 = t; sign -1 = forward (exp(-i..)), +1 = inverse. */
-void or_fft_axis(double complex *A, int Nx, int Ny, int Nt, int axis, int sign);
+void or_fft_axis(or_complex *A, int Nx, int Ny, int Nt, int axis, int sign);
 
 /* exp(dzz/2*(i*betas - alpha/2)) then fftshift (kernels.cu:47-54, propagation.c:150-156,393-402). */
-void or_expD0(double complex *out, int Nt, double dzz, double alpha, const double *betas);
+void or_expD0(or_complex *out, int Nt, double dzz, double alpha, const double *betas);
 
 /* Diffraction table and sign update (propagation.c:375-391).  n = table length,
  * nwr = length of wr (Ny).  dzh is the half step (the caller passes dzz/2). */
-void or_calcexpR(double complex *expR, int n, int nwr, int *signmem, double z, double Cav,
+void or_calcexpR(or_complex *expR, int n, int nwr, int *signmem, double z, double Cav,
                  double k0, double dzh, const double *wr, const or_switches *sw);
 
 /* Linear step (propagation.c:65-108, FFTW ordering with the A9 index fix). */
-void or_linearstep(double complex *A, int Nx, int Ny, int Nt, const double complex *expD0,
-                   const double complex *expRx, const double complex *expRy);
+void or_linearstep(or_complex *A, int Nx, int Ny, int Nt, const or_complex *expD0,
+                   const or_complex *expRx, const or_complex *expRy);
 
 /* Self-steepening term sst = gamma2/w0*(2 dA A* + A dA*), dA = IFFT_t[-i w FFT_t A]/Nt
  * (propagation.c:164-233). */
-void or_sst(const double complex *A, int Nx, int Ny, int Nt, const double *w, double gamma2,
-            double w0, double complex *sst);
+void or_sst(const or_complex *A, int Nx, int Ny, int Nt, const double *w, double gamma2,
+            double w0, or_complex *sst);
 
 void or_ionizpot(const char *gas, double *I1, double *I2);            /* plasma.c:4-40 */
 void or_Natoms(const char *gas, double *Natm, double *sigm_coll);     /* plasma.c:61-115 */
 void or_ADK(double *rates1, double *rates2, long n, const double *C_nl, const double *f_lm,
             const double *nq, const double *mq, const double *Ei, const double *E); /* plasma.c:43-58 */
 /* Ionization (plasma.c:118-245): outputs tau_c and freeelectrons_sp, N values each. */
-void or_ioniz(const double complex *A, int Nx, int Ny, int Nt, double w0, double deltat,
+void or_ioniz(const or_complex *A, int Nx, int Ny, int Nt, double w0, double deltat,
               const char *gas, double rho_c, const double *w, double rho_nt, double n0,
               double *tau_c, double *fe_sp, const or_switches *sw);
 
@@ -99,26 +104,31 @@ void or_ioniz(const double complex *A, int Nx, int Ny, int Nt, double w0, double
 void or_calc1oes(const double *BP, int n, const double *r, double *vald1oes, double *y);
 
 /* Beam profiles BP1[x] = sum_{y,t}|A|^2, BP2[y] = sum_{x,t}|A|^2 (propagation.c:343-354). */
-void or_beam_profiles(const double complex *A, int Nx, int Ny, int Nt, double *BP1, double *BP2);
+void or_beam_profiles(const or_complex *A, int Nx, int Ny, int Nt, double *BP1, double *BP2);
 
 /* One symmetric split step (propagation.c:111-372). */
-void or_ssfmprop(double complex *A, const or_params *p, double dzz, int *signmem, double z,
+void or_ssfmprop(or_complex *A, const or_params *p, double dzz, int *signmem, double z,
                  double *puls_e, double *BP1, double *BP2, double *y1, double *y2,
                  double *bps1, double *bps2, int change, const or_switches *sw);
 
+/* The dz rule of setStep (propagation.c:636-676) for a given local error err: writes dzz
+ * and bad.  y1, y2 are the beam-size records of calc1oes (y[1] caps the growth of dz). */
+void or_step_rule(double err, double *dzz, double def_err, double dzmin, const double *y1,
+                  const double *y2, int *bad);
+
 /* Step-size control (propagation.c:616-677).  Returns nothing; writes dzz, bad, err. */
-void or_setStep(long n, double *dzz, const double complex *C1, const double complex *C2,
+void or_setStep(long n, double *dzz, const or_complex *C1, const or_complex *C2,
                 double def_err, double dzmin, const double *y1, const double *y2, int *bad,
                 double *err);
 
 /* temp[k] = sum_xy |A|^2, spec[k] = sum_xy |FFT_t A|^2 in FFT order (MPC.c:389-449). */
-void or_diag(const double complex *A, int Nx, int Ny, int Nt, double *temp, double *spec);
+void or_diag(const or_complex *A, int Nx, int Ny, int Nt, double *temp, double *spec);
 
 /* Energy calibration (MPC.c:206-216): A *= sqrt(puls_e/Esig). */
-void or_calibrate(double complex *A, long n, double puls_e, double Esig, const or_switches *sw);
+void or_calibrate(or_complex *A, long n, double puls_e, double Esig, const or_switches *sw);
 
 /* Mirror lens phase exp(-i k0 (x^2+y^2)/roc) with x = r[i], y = r[j] (lens bounce mode). */
-void or_mirror_lens(double complex *A, int Nx, int Ny, int Nt, const double *r, double k0,
+void or_mirror_lens(or_complex *A, int Nx, int Ny, int Nt, const double *r, double k0,
                     double roc);
 
 /* Driver state carried between steps (MPC.c:234-238). */
@@ -130,12 +140,12 @@ typedef struct {
 
 /* Fixed-step run: nsteps calls of ssfmprop(dzz), z advancing by dzz each; in lens
  * mode the mirror phase is applied after each step that ends on a pass boundary. */
-void or_run_fixed(double complex *A, const or_params *p, or_state *st, int nsteps,
+void or_run_fixed(or_complex *A, const or_params *p, or_state *st, int nsteps,
                   const or_switches *sw);
 
 /* One step-doubling attempt (MPC.c:269-383 with the A4 fix: C1 = C2 = A first).
  * C1, C2 are N-sized work buffers.  On accept A = (4 C2 - C1)/3, z += 2 dzz. */
-void or_double_step(double complex *A, double complex *C1, double complex *C2,
+void or_double_step(or_complex *A, or_complex *C1, or_complex *C2,
                     const or_params *p, or_state *st, const or_switches *sw);
 
 #ifdef __cplusplus
