@@ -112,22 +112,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profile_traffic(name: str):
-    """dram bytes per launch of the dominant sweep from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        for ln in f:
-            if ln.startswith("traffic_bytes_per_launch:"):
-                return float(ln.split(":", 1)[1])
-    return None
+def profile_traffic(names):
+    """dram bytes per launch of a sweep from the committed ncu summaries of its kernels (summed
+    over the kernels of the sweep), or None when one is missing."""
+    total = 0.0
+    for name in names:
+        path = os.path.join(ROOT, "profiles", name)
+        if not os.path.exists(path):
+            return None
+        val = None
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    val = float(ln.split(":", 1)[1])
+        if val is None:
+            return None
+        total += val
+    return total
 
 
 WORKLOADS = {
     "cell256": dict(config="config2", adaptive=False, per_step=400, cpu_steps=5,
                     desc="multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
-                    step="one pass of the cell = 400 split steps", profile="pencil_step_256x256x2048.txt"),
+                    step="one pass of the cell = 400 split steps",
+                    profile={"pencil": ["pencil_step_256x256x2048.txt"],
+                             "plane": ["plane_y_256x256x2048.txt", "plane_x_256x256x2048.txt"]}),
     "cell64": dict(config="config1", adaptive=False, per_step=200, cpu_steps=100,
                    desc="multipass cell 64x64x512, fixed split steps, lens mirror, SST + ADK + plasma on",
                    step="one pass of the cell = 200 split steps", profile=None),
@@ -145,8 +154,9 @@ def make_workload(name: str = "cell256"):
     return cfg, p, A
 
 
-def cpu_baseline_run(p, A, nsteps: int, threads: int):
-    """The FP64 CPU restatement (oracle/) on `nsteps` split steps of the same cell."""
+def cpu_baseline_run(p, A, nsteps: int, threads: int, keep: bool = False):
+    """The FP64 CPU restatement (oracle/) on `nsteps` split steps of the same cell: the time,
+    and with keep the resulting field as well."""
     import oracle
     oracle.set_threads(threads)
     o = oracle.Oracle(p)
@@ -155,7 +165,45 @@ def cpu_baseline_run(p, A, nsteps: int, threads: int):
     st = o.new_state()
     t = time.perf_counter()
     o.run_fixed(B, st, nsteps)
-    return time.perf_counter() - t
+    dt = time.perf_counter() - t
+    return (dt, B) if keep else dt
+
+
+def _power_spectrum(A, p):
+    import torch
+    F = torch.fft.fft(torch.from_numpy(A.reshape(p.Nt, p.Ny * p.Nx)).cuda(), dim=0)
+    return (F.abs() ** 2).sum(dim=1).cpu().numpy()
+
+
+def accuracy_of(p, A, ref, nsteps: int, variant: int) -> dict:
+    """The device path's relative L2 errors after `nsteps` split steps from the same seeded,
+    calibrated field, against the FP64 oracle's field `ref` (the CPU baseline's own run)."""
+    from mpc_gb300 import capi
+    with capi.Propagator(p.copy(variant=variant)) as prop:
+        prop.upload(A, calibrate=True)
+        prop.run_fixed(nsteps)
+        got = prop.download()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    out = {"split_steps": nsteps, "against": "FP64 oracle (CPU), same seeded input",
+           "field_rel_l2": rel(got, ref), "spectrum_rel_l2": rel(_power_spectrum(got, p), _power_spectrum(ref, p))}
+    whole = whole_run_accuracy(p)
+    if whole:
+        out["whole_run"] = whole
+    return out
+
+
+def whole_run_accuracy(p):
+    """The whole run's errors against the FP64 GPU oracle from the committed report, if any."""
+    path = os.path.join(ROOT, "profiles", f"accuracy_whole_run_{p.Nx}x{p.Ny}x{p.Nt}.txt")
+    if not os.path.exists(path):
+        return None
+    out = {"source": os.path.relpath(path, ROOT)}
+    with open(path) as f:
+        for ln in f:
+            for key in ("split_steps", "field_rel_l2", "spectrum_rel_l2", "energy_drift"):
+                if ln.startswith(key + ":"):
+                    out[key] = float(ln.split(":", 1)[1])
+    return out
 
 
 def dist_init():
@@ -263,10 +311,12 @@ def run_gb300(args):
     sweeps = {"pencil": (kt["pencil_ms"], kt["n_pencil"]), "plane": (kt["plane_ms"], kt["n_plane"])}
     dom = max(sweeps, key=lambda k: sweeps[k][0])
     dom_ms = sweeps[dom][0] / max(1, sweeps[dom][1])
-    bytes_launch = 16.0 * p.N  # one complex64 read + write of the whole field
+    # one complex64 read + write of the whole field per kernel; the plane sweep of the two-pass
+    # variants is two kernels (column strips, then row strips)
+    passes = vinfo.get("PL", 1) if dom == "plane" else 1
+    bytes_launch = 16.0 * p.N * passes
     achieved = bytes_launch / (dom_ms / 1e3) / 1e9
-    prof_name = {"pencil": "pencil_step_256x256x2048.txt", "plane": "plane_256x256x2048.txt"}[dom]
-    traffic = profile_traffic(prof_name) if wl["profile"] else None
+    traffic = profile_traffic(wl["profile"][dom]) if wl["profile"] else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": traffic, "kernel": f"{dom} sweep",
                 "peak_source": src, "per_sweep_ms": {k: v[0] / max(1, v[1]) for k, v in sweeps.items()},
@@ -284,13 +334,34 @@ def run_gb300(args):
     e2e = {"value": p.N * e2e_split * world / e2e_s, "unit": "grid-point-steps/s",
            "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N}
 
+    # the reference-signature drop-in: mpc_ssfmprop on a host field (pinned), one split step per
+    # call with the complex128 field copied in and out every call, as MPC.c's loop would call it
+    dropin = None
+    if not wl["adaptive"]:
+        st0 = prop.state()
+        prop.ssfmprop(pin.array, p.dzz, 1, 0.0, p.puls_e)
+        prop.sync()
+        ncall = 5
+        t0 = time.perf_counter()
+        for _ in range(ncall):
+            prop.ssfmprop(pin.array, p.dzz, 1, 0.0, p.puls_e)
+        dt_call = (time.perf_counter() - t0) / ncall
+        prop.set_state(st0)
+        dropin = {"value": p.N * world / dt_call, "unit": "grid-point-steps/s", "ms_per_split_step": dt_call * 1e3,
+                  "api": "mpc_ssfmprop on a pinned host complex128 field, one split step per call",
+                  "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N}
+
     cpu = None
+    accuracy = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         nst = wl["cpu_steps"]  # about 10 s on 16 host cores
-        dt = cpu_baseline_run(p, A, nst, cores)
+        dt, Bref = cpu_baseline_run(p, A, nst, cores, keep=True)
         cpu = {"value": p.N * nst / dt, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
                "sample": f"{nst} split steps of the {p.Nx}x{p.Ny}x{p.Nt} cell, FP64 oracle/ restatement, OpenMP"}
+        if not wl["adaptive"]:
+            accuracy = accuracy_of(p, A, Bref, nst, args.variant)
+        del Bref
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     fp32_peak = nsm * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
     fft_tflops = (value / world) * fft_flop_per_pt_step(p.Nx, p.Ny, p.Nt) / 1e12
@@ -308,7 +379,7 @@ def run_gb300(args):
                                   "field fits L2: the bench step's passes re-read it from L2"),
                            "parallelism": f"replicas x{world}", "kernel_variant": vinfo},
                 "roofline": roofline, "fft_rate": fft_rate, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clk}
+                "dropin": dropin, "accuracy": accuracy, "gpu_launches": launches, "clocks": clk}
         if wl["adaptive"]:
             line["accepted_pt_steps_per_s"] = accepted_rate
         print(json.dumps(line), flush=True)
@@ -318,17 +389,44 @@ def run_gb300(args):
         dist.barrier()
 
 
-def run_profile_case(nsteps: int, variant: int = 0, workload: str = "cell256"):
+def run_profile_case(nsteps: int, variant: int = 0, workload: str = "cell256", all_kernels: bool = False):
     """A short target for ncu: upload the workload's field and run `nsteps` split steps,
     with no timing.  Launch order: the entry pencil sweep (template mode 0), then per split
-    step one pencil sweep (mode 2) and one plane sweep."""
+    step one pencil sweep (mode 2) and one plane sweep.  With all_kernels, then every other
+    kernel of the library once: one step-doubling attempt (k_richardson,
+    k_pencil_energy_slots, k_beam_profiles), the diagnostics (pencil mode 5, k_spec), the
+    step-size features (k_moments), the controller network's inference, loss gradient and one
+    training epoch (k_mlp_predict, k_mlp_grad, k_adam), and the allocation-free nonlinear step
+    (k_nonlinear_noalloc) on a complex64 copy of the field."""
     from mpc_gb300 import capi
     cfg, p, A = make_workload(workload)
     with capi.Propagator(p.copy(variant=variant)) as prop:
         prop.upload(A, calibrate=True)
+        B = prop.download() if all_kernels else None   # the calibrated field, for the noalloc step
         prop.run_fixed(nsteps)
         prop.sync()
+        if all_kernels:
+            prop.step_double()
+            prop.diag()
+            prop.features()
+            prop.sync()
         print(json.dumps({"profile_case": nsteps, "grid": [p.Nx, p.Ny, p.Nt], "launches": prop.launch_count()}))
+    if all_kernels:
+        import torch
+        from mpc_gb300 import dzlearn
+        mlp = dzlearn.load()
+        rng = np.random.default_rng(0)
+        X = rng.standard_normal((4096, capi.NFEATURES)).astype(np.float32)
+        y = rng.standard_normal(4096).astype(np.float32)
+        mlp.predict(X)
+        mlp.loss_grad(X, y)
+        mlp.train(X, y, epochs=1, batch=256)
+        mlp.close()
+        if p.Nt <= 2048:
+            dev = torch.from_numpy(B.astype(np.complex64)).to("cuda")
+            rc = capi.nonlinear_noalloc(p, dev.data_ptr(), p.dzz, torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            print(json.dumps({"noalloc_status": rc}))
 
 
 def main():
@@ -344,9 +442,11 @@ def main():
                          "serialised timings mislead the autotuner)")
     ap.add_argument("--profile-case", type=int, default=0, metavar="NSTEPS",
                     help="run NSTEPS split steps of the workload and exit (an ncu target)")
+    ap.add_argument("--all-kernels", action="store_true",
+                    help="with --profile-case: then launch every other kernel of the library once")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case, max(args.variant, 0), args.workload)
+        run_profile_case(args.profile_case, max(args.variant, 0), args.workload, args.all_kernels)
     elif args.impl == "reference":
         run_reference(args)
     else:

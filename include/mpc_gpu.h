@@ -30,7 +30,8 @@ enum {
     MPC_ERR_NONFINITE = 5,  /* the field became NaN/Inf */
     MPC_ERR_STATE = 6,      /* call out of order (e.g. no field uploaded) */
     MPC_ERR_IO = 7,         /* file could not be read/written */
-    MPC_ERR_UNSUPPORTED = 8 /* option not implemented on the device path */
+    MPC_ERR_UNSUPPORTED = 8, /* option not implemented on the device path */
+    MPC_ERR_TIMEOUT = 9     /* a bounded device-side wait ran out; the kernel stopped early */
 };
 
 enum { MPC_BOUNCE_SIGNFLIP = 0, MPC_BOUNCE_LENS = 1 };
@@ -257,6 +258,14 @@ int mpc_variant_info(mpc_ctx *ctx, int *variant, int info[10]);
 int mpc_profile(mpc_ctx *ctx, int on);
 int mpc_kernel_times(mpc_ctx *ctx, double *pencil_ms, long *n_pencil, double *plane_ms, long *n_plane);
 
+/* Self-check of the bounded device-side waits (no counterpart in the reference): launches a
+ * one-thread kernel that waits on an mbarrier nothing completes.  The wait gives up after about
+ * a second and leaves its code in the context's kernel error word, which this call reads and
+ * clears: it returns MPC_ERR_TIMEOUT when the limit works, and the context stays usable.  Every
+ * wait of the library's TMA-staged kernels is bounded the same way; mpc_sync and
+ * mpc_field_download report such a timeout as MPC_ERR_TIMEOUT. */
+int mpc_wait_limit_check(mpc_ctx *ctx);
+
 /* ---- allocation-free nonlinear step (no counterpart in the reference) -------------- */
 /* The nonlinear half of a split step, A *= exp(dz * A_nl(A)) with Kerr, self-steepening,
  * ionization and plasma terms, applied in place to a field the caller already holds in
@@ -269,17 +278,19 @@ int mpc_kernel_times(mpc_ctx *ctx, double *pencil_ms, long *n_pencil, double *pl
  * allocate), processes whose device memory is owned entirely by a pool handed out at
  * start-up, hosts with a fixed device-memory budget -- this call allocates nothing: no
  * cudaMalloc, no cudaFree, no context.  Its work buffers are one static device array of
- * 8,445,952 bytes inside libmpc_gpu.so, which every GPU that loads the library holds
+ * 8,429,568 bytes inside libmpc_gpu.so, which every GPU that loads the library holds
  * until the process exits.  Limits: Nt one of 64, 256, 512, 1024, 2048 (at most 2048),
  * Nx*Ny a multiple of 16384/Nt; larger or other sizes are rejected with MPC_ERR_SHAPE.
  *
- * The first call on a device looks up the device address of that array (and sets the
- * kernel's shared-memory limit) with that device current; make the first call before any
- * stream capture.  Every call shares the array and leaves its contents behind; nothing in
- * it needs to start at zero (each call rewrites what it reads).  Calls that overlap on the
- * GPU -- on different streams, or from several host threads -- race on the array.  The
- * work is queued on `stream` (a cudaStream_t, NULL for the legacy stream) and the call
- * returns without waiting; errors are printed to stderr and returned as MPC_ERR_*. */
+ * Every call looks up the device address of that array on the current device (an
+ * allocation-free runtime query) and passes the omega grid to the device by value, so the
+ * call keeps no pointer to p or its arrays after it returns.  The first call on a device
+ * loads the library's device code: make it before any stream capture begins.  Every call
+ * shares the array and leaves its contents behind; nothing in it needs to start at zero
+ * (each call rewrites what it reads).  Calls that overlap on the GPU -- on different
+ * streams, or from several host threads -- race on the array.  The work is queued on
+ * `stream` (a cudaStream_t, NULL for the legacy stream) and the call returns without
+ * waiting; errors are printed to stderr and returned as MPC_ERR_*. */
 int mpc_nonlinear_noalloc(const mpc_params *p, void *A_dev, double dz, void *stream);
 
 #ifdef __cplusplus

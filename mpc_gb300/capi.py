@@ -18,7 +18,7 @@ LIB_PATH = os.environ.get("MPC_GPU_LIB", os.path.join(_HERE, "libmpc_gpu.so"))
 
 MPC_OK = 0
 ERRORS = {1: "MPC_ERR_ARG", 2: "MPC_ERR_SHAPE", 3: "MPC_ERR_CUDA", 4: "MPC_ERR_NOMEM", 5: "MPC_ERR_NONFINITE",
-          6: "MPC_ERR_STATE", 7: "MPC_ERR_IO", 8: "MPC_ERR_UNSUPPORTED"}
+          6: "MPC_ERR_STATE", 7: "MPC_ERR_IO", 8: "MPC_ERR_UNSUPPORTED", 9: "MPC_ERR_TIMEOUT"}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -74,6 +74,7 @@ SIGNATURES = {
     "mpc_variant_info": (C.c_int, [C.c_void_p, _ip, _ip]),
     "mpc_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "mpc_kernel_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long), _dp, C.POINTER(C.c_long)]),
+    "mpc_wait_limit_check": (C.c_int, [C.c_void_p]),
     "mpc_nonlinear_noalloc": (C.c_int, [C.POINTER(c_mpc_params), C.c_void_p, C.c_double, C.c_void_p]),
     "mpc_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "mpc_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/mpc_gpu.h"
+#include "mpc_nlsetup.h"
 #include "mpc_shapes.cuh"
 
 using mpc::NLConst;
@@ -35,12 +36,10 @@ extern const ShapeOps* const shape_list_c[];
 extern const ShapeOps* const shape_list_d[];
 }  // namespace mpc
 
-// constants.h:1-11
-static const double ZW0 = 377.0, NC = 1.0, FCTR = 0.89, IH = 27.21, EF = 5.14220642e11;
-static const double ME = 9.1094e-31, EL0 = 1.602e-19, NAVO = 6.02214e+23, T0 = 2.4188843265e-17;
-static const double C0 = 299792458.0, HBAR = 1.054560652926899e-34;
+// constants.h:1-11 (mpc_nlsetup.h)
+static const double HBAR = mpc::kHBAR;
 // device units: |a|^2 = intensity / I_UNIT
-static const double I_UNIT = 1e16;
+static const double I_UNIT = mpc::kIUnit;
 
 static thread_local std::string g_err;
 static int fail(int code, const char* what, cudaError_t e = cudaSuccess) {
@@ -305,7 +304,8 @@ struct mpc_ctx {
     float2 *twx = nullptr, *twy = nullptr, *twt = nullptr;  // packed twiddle tables
     float2 *C1 = nullptr, *C2 = nullptr;                    // step doubling (allocated on first use)
     double* hsd = nullptr;   // pinned: error sums and C2's beam profiles of the last attempt (2 + Nx + Ny)
-    unsigned int* dstats = nullptr;  // running maxima of the split steps since the last reset (4)
+    unsigned int* dstats = nullptr;  // running maxima of the split steps since the last reset (4),
+                                     // then at dstats[4] the kernels' error word
     double* dmom = nullptr;          // field moments (7 doubles) and max |S|^2 (bits, after them)
     double sd_dz = 0.0;      // dz of the attempt in flight
     double sd_natural = 0.0; // the step before landing on a mirror plane shortened it
@@ -403,73 +403,16 @@ static int upload_twiddles(int N, float2** d) {
 
 static int pass_sign(double z, double Cav) { return ((int)(floor(z / Cav) + 1) % 2) * 2 - 1; }
 
-// ionizpot (plasma.c:4-40) and Natoms (plasma.c:61-115)
-static int gas_tables(const char* gas, double* I1, double* I2, double* Natm, double* sig) {
-    struct G { const char* n; double i1, i2, dens, M, sig; };
-    static const G g[] = {
-        {"Argon", 15.75962, 27.62967, 1.784 * 1e3, 39.941, 1.57e-20},
-        {"Helium", 24.58741, 54.41778, 0.166e3, 4.002602, 6.11e-20},
-        {"Neon", 21.5646, 40.96328, 0.9002e3, 20.1797, 1.65e-20},
-        {"Air", 0.78084 * 14.53414 + 0.20946 * 13.61806 + 0.00934 * 15.75962,
-         0.78084 * 29.6013 + 0.20946 * 35.11730 + 0.00934 * 27.62967, 1.205e3, 28.97, 10e-20},
-        {"Nitrogen", 14.53414, 29.6013, 1.65e3, 14.0067, 10.2e-20},
-        {"Xenon", 12.1298, 21.20979, 5.86e3, 5.761, 3.55e-20},
-        {"Krypton", 13.99961, 24.35985, 3.749e3, 83.798, 1.15e-20},
-    };
-    for (const G& e : g)
-        if (strcmp(gas, e.n) == 0) {
-            *I1 = e.i1;
-            *I2 = e.i2;
-            *Natm = e.dens * NAVO / e.M;
-            *sig = e.sig;
-            return 1;
-        }
-    return 0;
-}
-
 // FP32 constants of the fused nonlinear step (plasma.c:118-245, propagation.c:244-327;
-// A11 and A18 corrections applied)
+// A11 and A18 corrections applied), from the setup shared with mpc_noalloc.cu
 static void build_nl(mpc_ctx* c) {
-    const mpc_params& p = c->p;
-    NLConst& n = c->nl;
-    memset(&n, 0, sizeof n);
-    const double fs2 = c->fs * c->fs;
-    n.gam = (float)(p.gamma2 / fs2);
-    c->sst_c_full = (float)(p.gamma2 / (p.w0 * fs2));
-    n.sst_c = p.sst_on == 1 ? c->sst_c_full : 0.0f;
-    n.I_scale = (float)I_UNIT;
-    const double E_c = sqrt(2.0 * ZW0 / NC) * FCTR / EF;  // plasma.c:145-149
-    n.E_c = (float)E_c;
-    n.inv_E_c = (float)(1.0 / E_c);
-    double I1 = 0, I2 = 0, Natm = 0, sig = 0;
-    c->ion_gas_ok = gas_tables(p.gas, &I1, &I2, &Natm, &sig);
-    c->I1 = I1;
-    c->I2 = I2;
-    const double Iion[2] = {I1 / IH, I2 / IH};
-    const double nq[2] = {1.0 / sqrt(2.0 * Iion[0]), 2.0 / sqrt(2.0 * Iion[1])};
-    double K1[2], K3[2], K5[2];
-    for (int s = 0; s < 2; s++) {
-        const double Cnl = sqrt(pow(2.0, 2.0 * nq[s]) / (nq[s] * tgamma(nq[s] + 1.0) * tgamma(nq[s])));
-        K1[s] = Cnl * Cnl * sqrt(6.0 / M_PI) * 1.0 * Iion[s];
-        K3[s] = 2.0 * pow(2.0 * Iion[s], 1.5);
-        K5[s] = 2.0 * nq[s] - 0.0 - 1.5;
-        n.l2K1[s] = (float)log2(K1[s]);
-        n.l2K3[s] = (float)log2(K3[s]);
-        n.K5[s] = (float)K5[s];
-        n.K3l2e[s] = (float)(K3[s] / (3.0 * M_LN2));
-    }
-    c->adk = ADKConst{K1[0], K1[1], K3[0], K3[1], K5[0], K5[1]};
-    const double Kon = p.deltat / T0;
-    n.Kon = (float)Kon;
-    // v_e = sqrt(2 e^2 E0^2 / (4 me^2 w0^2)) with E0 = F EF (plasma.c:203, A18: w0 only)
-    n.Kuv = (float)(sig * p.rho_nt * EL0 * EF / (sqrt(2.0) * ME * p.w0));
-    const double k0ion = p.w0 / C0;  // plasma.c:141
-    n.K4w0 = (float)(k0ion / (p.n0 * p.rho_c) * p.w0 * p.w0);
-    n.w0sq = (float)(p.w0 * p.w0);
-    n.inv_w0 = (float)(1.0 / p.w0);
-    n.invI1_Kon = I1 > 0 ? (float)(Kon / I1) : 0.0f;
-    n.rho_half = (float)(p.rho_nt / 2.0);
-    n.plasma = (p.plasm == 1) ? 1 : 0;
+    const mpc::NLSetup s = mpc::nl_setup(c->p, c->fs);
+    c->nl = s.nl;
+    c->sst_c_full = s.sst_c_full;
+    c->ion_gas_ok = s.gas_ok;
+    c->I1 = s.I1;
+    c->I2 = s.I2;
+    c->adk = ADKConst{s.K1[0], s.K1[1], s.K3[0], s.K3[1], s.K5[0], s.K5[1]};
 }
 
 // one allocation: FP64 factors (Nx + Ny + Nt double2), double-float Rx (Nx) and RyD (Ny*Nt)
@@ -556,6 +499,7 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     }
     a.lensx = c->lensx;
     a.lensy = c->lensy;
+    a.err = c->dstats + 4;
     a.Nt = c->Nt;
     a.NP = (int)c->NP;
     a.nunits = c->ops->SLO == 2 ? c->Nt / 2 : c->Nt / c->ops->PB;
@@ -563,7 +507,7 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     prof_begin(c, 1, &ev);
     CK(c->ops->plane(a, c->plane_clusters, c->st), "plane kernel launch");
     prof_end(c, 1, ev);
-    c->launches += c->ops->PL == 2 ? 2 + a.lens : 1;
+    c->launches += c->ops->PL >= 2 ? 2 + a.lens : 1;
     return MPC_OK;
 }
 
@@ -716,8 +660,9 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
     TRYC(cudaMalloc(&c->penergy, sizeof(double) * c->NP), "cudaMalloc pencil energies");
     // reductions: temp [0, Nt), spec [Nt, 2 Nt), beam profiles and sums use the front
     TRYC(cudaMalloc(&c->dred, sizeof(double) * (2 * Nt + Nx + Ny + 64)), "cudaMalloc reductions");
-    TRYC(cudaMalloc(&c->dstats, 4 * sizeof(unsigned int)), "cudaMalloc step statistics");
-    TRYC(cudaMemsetAsync(c->dstats, 0, 4 * sizeof(unsigned int), c->st), "memset step statistics");
+    // four running maxima, then the kernels' error word (KernelError)
+    TRYC(cudaMalloc(&c->dstats, 8 * sizeof(unsigned int)), "cudaMalloc step statistics");
+    TRYC(cudaMemsetAsync(c->dstats, 0, 8 * sizeof(unsigned int), c->st), "memset step statistics");
     TRYC(cudaMalloc(&c->dmom, 8 * sizeof(double)), "cudaMalloc field moments");
     {
         TRY(alloc_tables(c, &c->ident));
@@ -804,10 +749,40 @@ int mpc_variant_info(mpc_ctx* c, int* variant, int* info) {
     return MPC_OK;
 }
 
+// The wait-limit probe: one thread waits on an mbarrier that no copy and no thread completes; the
+// bounded wait gives up after kWaitLimitCycles and the kernel leaves KERR_WAIT_PROBE in *err.
+__global__ void k_wait_limit_probe(unsigned int* err) {
+    __shared__ uint64_t bar;
+    mpc::mbar_init(&bar, 1);
+    mpc::fence_mbar_init();
+    if (!mpc::mbar_wait(&bar, 0)) atomicExch(err, mpc::KERR_WAIT_PROBE);
+}
+
+// After a stream synchronisation: a kernel that gave up a bounded wait left its code in the
+// error word (the field is then incomplete).  The word is cleared once reported.
+static int kernel_errors(mpc_ctx* c) {
+    unsigned int w = 0;
+    CK(cudaMemcpy(&w, c->dstats + 4, sizeof w, cudaMemcpyDeviceToHost), "D2H kernel error word");
+    if (w == mpc::KERR_NONE) return MPC_OK;
+    CK(cudaMemset(c->dstats + 4, 0, sizeof w), "clear kernel error word");
+    return fail(MPC_ERR_TIMEOUT, w == mpc::KERR_TMA_TIMEOUT   ? "a bulk tensor load did not arrive within the wait limit"
+                                 : w == mpc::KERR_WAIT_PROBE ? "the wait-limit probe's wait ran out"
+                                                             : "kernel error word set");
+}
+
+int mpc_wait_limit_check(mpc_ctx* c) {
+    if (!c) return fail(MPC_ERR_ARG, "null context");
+    k_wait_limit_probe<<<1, 1, 0, c->st>>>(c->dstats + 4);
+    CK(cudaGetLastError(), "k_wait_limit_probe");
+    c->launches++;
+    CK(cudaStreamSynchronize(c->st), "wait-limit probe");
+    return kernel_errors(c);
+}
+
 int mpc_sync(mpc_ctx* c) {
     if (!c) return fail(MPC_ERR_ARG, "null context");
     CK(cudaStreamSynchronize(c->st), "stream synchronize");
-    return MPC_OK;
+    return kernel_errors(c);
 }
 
 int mpc_host_alloc(void** ptr, size_t bytes) {
@@ -903,7 +878,7 @@ int mpc_field_download(mpc_ctx* c, double* A) {
     if (rc) return rc;
     CK(cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H field");
     CK(cudaStreamSynchronize(c->st), "download");
-    return MPC_OK;
+    return kernel_errors(c);
 }
 
 // one nonlinear step of the pencil sweep, in place on buf (default: the field S)

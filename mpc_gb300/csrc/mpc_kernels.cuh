@@ -17,10 +17,12 @@
 //   kernels without clusters, the y part on column strips and the x part on row strips.
 #pragma once
 #include <cooperative_groups.h>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "mpc_fft.cuh"
+#include "mpc_tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -219,6 +221,9 @@ struct IonPoint {
     float sigma;     // K4 tau_c / (1 + w0^2 tau_c^2)
     float u;         // 1 / tau_c = sigma_coll rho_nt v_e
 };
+// SECOND = false: the second stage is known to flush to zero for every sample of the tile (the
+// first walk's test), so its rate is not evaluated and c2 = 0, the value it would flush to.
+template <bool SECOND = true>
 __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
     IonPoint r;
     float I = fmaf(a.x, a.x, a.y * a.y) * c.I_scale;
@@ -227,9 +232,9 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
     const float F = I * rs * c.E_c;              // |E| in atomic units
     const float invF = rs * c.inv_E_c;
     const float l2F = __log2f(F);
-    float w[2];
+    float w[2] = {0.0f, 0.0f};
 #pragma unroll
-    for (int st = 0; st < 2; st++) {
+    for (int st = 0; st < (SECOND ? 2 : 1); st++) {
         const float e2 = c.l2K1[st] + c.K5[st] * (c.l2K3[st] - l2F) - c.K3l2e[st] * invF;
         w[st] = (e2 > -126.0f) ? exp2f(e2) : 0.0f;
     }
@@ -240,8 +245,12 @@ __device__ __forceinline__ IonPoint ion_point(float2 a, const NLConst& c) {
     r.u = u;
     r.a = w[0] * c.Kon;
     r.b = r.sigma * I * c.invI1_Kon;
-    const float c2 = w[1] * c.Kon;
-    r.c2 = (c2 >= kC2Flush) ? c2 : 0.0f;
+    if constexpr (SECOND) {
+        const float c2 = w[1] * c.Kon;
+        r.c2 = (c2 >= kC2Flush) ? c2 : 0.0f;
+    } else {
+        r.c2 = 0.0f;
+    }
     return r;
 }
 
@@ -321,7 +330,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             float m00 = 1.f, m01 = 0.f, m10 = 0.f, m11 = 1.f, o0 = 0.f, o1 = 0.f;
 #pragma unroll 4
             for (int i = 0; i < CH; i++) {
-                const IonPoint ip = ion_point(s[V::at(t0 + i, p)], c);
+                const IonPoint ip = ion_point<true>(s[V::at(t0 + i, p)], c);
                 R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
                 const float g = one_minus_exp_neg(R);
                 const float n00 = fmaf(ip.c2, m10, m00), n01 = fmaf(ip.c2, m11, m01);
@@ -341,50 +350,56 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
             v = (float)muv[p * TPP + ch].o1;
         }
         // S3: apply the nonlinear step (or emit the ionization outputs).  The dA samples come
-        // from L2: a ring of kDAPrefetch registers loads each kDAPrefetch samples ahead.
-        float R = Rin;
-        float2 ring[kDAPrefetch];
-        if (!IONIZ_ONLY && c.sst_c != 0.0f) {
-#pragma unroll
-            for (int k = 0; k < kDAPrefetch; k++) ring[k] = dA[k * P];
-        }
-#pragma unroll kDAPrefetch
-        for (int i = 0; i < CH; i++) {
-            const int t = t0 + i;
-            float2 dAi = make_float2(0.0f, 0.0f);
+        // from L2: a ring of kDAPrefetch registers loads each kDAPrefetch samples ahead.  Tiles
+        // without second-stage ionization (any2 == 0) take the walk without the second rate.
+        auto walk = [&](auto second) {
+            constexpr bool SECOND = decltype(second)::value;
+            float R = Rin;
+            float2 ring[kDAPrefetch];
             if (!IONIZ_ONLY && c.sst_c != 0.0f) {
-                dAi = ring[i % kDAPrefetch];
-                if (i + kDAPrefetch < CH) ring[i % kDAPrefetch] = dA[(i + kDAPrefetch) * P];
+#pragma unroll
+                for (int k = 0; k < kDAPrefetch; k++) ring[k] = dA[k * P];
             }
-            const float2 a = w[V::walk(i)];
-            const IonPoint ip = ion_point(a, c);
-            R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
-            const float g = one_minus_exp_neg(R);
-            const float ions = fmaf(2.0f, u, v);     // state before slice t (plasma.c:238-241)
-            const float nu = fmaf(ip.c2, v, u);
-            v = g - u;
-            u = nu;
-            if constexpr (IONIZ_ONLY) {
-                const size_t gi = (size_t)t * NP + q0 + p;
-                tau_out[gi] = 1.0 / (double)ip.u;
-                fe_out[gi] = (double)ions * (double)ip.sigma;
-                continue;
+#pragma unroll kDAPrefetch
+            for (int i = 0; i < CH; i++) {
+                const int t = t0 + i;
+                float2 dAi = make_float2(0.0f, 0.0f);
+                if (!IONIZ_ONLY && c.sst_c != 0.0f) {
+                    dAi = ring[i % kDAPrefetch];
+                    if (i + kDAPrefetch < CH) ring[i % kDAPrefetch] = dA[(i + kDAPrefetch) * P];
+                }
+                const float2 a = w[V::walk(i)];
+                const IonPoint ip = ion_point<SECOND>(a, c);
+                R = fmaf(1.0f - ip.b, R + ip.a, ip.b);
+                const float g = one_minus_exp_neg(R);
+                const float ions = fmaf(2.0f, u, v);     // state before slice t (plasma.c:238-241)
+                const float nu = fmaf(ip.c2, v, u);
+                v = g - u;
+                u = nu;
+                if constexpr (IONIZ_ONLY) {
+                    const size_t gi = (size_t)t * NP + q0 + p;
+                    tau_out[gi] = 1.0 / (double)ip.u;
+                    fe_out[gi] = (double)ions * (double)ip.sigma;
+                    continue;
+                }
+                const float pl = c.rho_half * ions;
+                const float a2 = fmaf(a.x, a.x, a.y * a.y);
+                float re = -pl * ip.sigma;
+                float im = fmaf(c.gam, a2, -pl * ip.qw);
+                if (c.sst_c != 0.0f) {
+                    const float2 sd = cmulc(dAi, a);  // dA * conj(A)
+                    re = fmaf(-3.0f * c.sst_c, sd.x, re);
+                    im = fmaf(-c.sst_c, sd.y, im);
+                }
+                const float amp = exp_small(c.dz * re);
+                float sn, cs;
+                sincos_small(c.dz * im, &sn, &cs);
+                w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
+                mx = make_float4(fmaxf(mx.x, a2), fmaxf(mx.y, ions), fmaxf(mx.z, fabsf(im)), fmaxf(mx.w, fabsf(re)));
             }
-            const float pl = c.rho_half * ions;
-            const float a2 = fmaf(a.x, a.x, a.y * a.y);
-            float re = -pl * ip.sigma;
-            float im = fmaf(c.gam, a2, -pl * ip.qw);
-            if (c.sst_c != 0.0f) {
-                const float2 sd = cmulc(dAi, a);  // dA * conj(A)
-                re = fmaf(-3.0f * c.sst_c, sd.x, re);
-                im = fmaf(-c.sst_c, sd.y, im);
-            }
-            const float amp = exp_small(c.dz * re);
-            float sn, cs;
-            sincos_small(c.dz * im, &sn, &cs);
-            w[V::walk(i)] = cmul(a, make_float2(amp * cs, amp * sn));
-            mx = make_float4(fmaxf(mx.x, a2), fmaxf(mx.y, ions), fmaxf(mx.z, fabsf(im)), fmaxf(mx.w, fabsf(re)));
-        }
+        };
+        if (any2) walk(std::true_type{});
+        else walk(std::false_type{});
     } else {
         float2 ring[kDAPrefetch];
         if (c.sst_c != 0.0f) {
@@ -779,6 +794,7 @@ struct PlaneArgs {
     int Nt;
     int NP;
     int nunits;          // number of cluster work units
+    unsigned int* err;   // error word of the TMA-staged kernels (KernelError), device memory
 };
 
 template <int NX, int NY, int CL, int PB, int SLO>
@@ -1067,6 +1083,241 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_y_ke
         }
         __syncthreads();
     }
+}
+
+// y part with TMA staging: a persistent CTA walks its units (slot, strip of CXS columns) with
+// NBUF unit buffers in shared memory; one thread keeps NBUF - 1 units in flight as 2-D bulk tensor
+// loads (box: CXS complex columns x NY rows of one omega-plane, landing in the StripYView layout),
+// and each finished unit leaves by a bulk tensor store, so no thread spends instructions or
+// registers on moving the strips.  tin / tout map the field as float rows of 2 Nx values, Ny * Nt
+// rows.  A load that does not arrive within the wait limit sets *err and ends the kernel.
+template <int NX, int NY, int CXS>
+struct StripYTmaCfg {
+    static constexpr int UNIT_BYTES = NY * CXS * 8;
+    static_assert(UNIT_BYTES % 128 == 0 && CXS * 8 % 16 == 0, "unit buffers of whole 128 B lines");
+    static constexpr __host__ __device__ int TW_OFF(int nbuf) { return nbuf * UNIT_BYTES; }
+    static constexpr __host__ __device__ int BAR_OFF(int nbuf) { return TW_OFF(nbuf) + ((twiddle_bytes(NY) + 15) / 16) * 16; }
+    static constexpr __host__ __device__ int SMEM(int nbuf) { return 128 + BAR_OFF(nbuf) + nbuf * 8 + 16; }
+};
+
+template <int NX, int NY, int CXS, int NTHR, int NBUF>
+__global__ void __launch_bounds__(NTHR, 512 / NTHR)
+    plane_y_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, PlaneArgs a,
+                       int second, unsigned int* err) {
+    using C = StripYTmaCfg<NX, NY, CXS>;
+    using V = StripYView<NY, CXS>;
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    // unit buffers on a 128-byte boundary of the shared window (the launch adds 128 B of slack)
+    unsigned char* smem_raw = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
+    unsigned char* tw_mem = smem_raw + C::TW_OFF(NBUF);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + C::BAR_OFF(NBUF));
+    int& s_arrived = *reinterpret_cast<int*>(bars + NBUF);
+    const int tid = threadIdx.x;
+    constexpr int STRIPS = NX / CXS;
+    const int units = a.Nt * STRIPS;
+    const int nmine = blockIdx.x < units ? (units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int b = 0; b < NBUF; b++) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+    }
+    stage_twiddles<NY, NTHR>(tw_mem, a.twy, tid);
+    const Twiddles tw = Twiddles::packed(tw_mem, NY);
+    const float4* RyD = second ? a.t2.RyD : a.t1.RyD;
+    __syncthreads();
+    auto buf = [&](int k) { return reinterpret_cast<float2*>(smem_raw + (k % NBUF) * C::UNIT_BYTES); };
+    auto issue = [&](int k) {   // load my k-th unit
+        const int unit = (int)blockIdx.x + k * (int)gridDim.x;
+        const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
+        mbar_arrive_expect_tx(&bars[k % NBUF], C::UNIT_BYTES);
+        tma_load_2d(buf(k), &tin, 2 * x0, slot * NY, &bars[k % NBUF]);
+    };
+    if (tid == 0)
+        for (int k = 0; k < NBUF - 1 && k < nmine; k++) issue(k);
+    for (int k = 0; k < nmine; k++) {
+        const int unit = (int)blockIdx.x + k * (int)gridDim.x;
+        const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
+        // one thread decides whether the unit arrived in time, so that the whole CTA takes the
+        // same branch; then every thread observes the completed phase itself
+        if (tid == 0) s_arrived = mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1)) ? 1 : 0;
+        __syncthreads();
+        if (!s_arrived) {
+            if (tid == 0) {
+                atomicExch(err, KERR_TMA_TIMEOUT);
+                // the loads still in flight target the later buffers: wait (bounded) for them
+                for (int j = k + 1; j < k + NBUF - 1 && j < nmine; j++) mbar_wait(&bars[j % NBUF], (uint32_t)((j / NBUF) & 1));
+                bulk_wait<0>();
+            }
+            return;
+        }
+        mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1));   // completed: returns at once
+        float2* s = buf(k);
+        dif_op_dit<NY, NY, V, NTHR, 1>(s, tw, tid, YSlotFactors{RyD, a.Nt, slot});
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_2d(&tout, 2 * x0, slot * NY, s);
+            bulk_commit();
+            if (k + NBUF - 1 < nmine) {
+                bulk_wait_read<1>();   // the previous unit's store has left its buffer
+                issue(k + NBUF - 1);
+            }
+        }
+    }
+    if (tid == 0) bulk_wait<0>();
+}
+
+// x part with TMA staging, for rows of 256 = 16 x 16 points.  A unit is 16 rows of one omega-plane
+// (32 KB, contiguous in HBM), loaded as 16 boxes of 16 rows x 16 complex (128 B box rows) with the
+// 128-byte swizzle: box b (x = 16 b .. 16 b + 15) lands at byte 2048 b, row l at 128 l within it,
+// and the 16-byte chunk c of the row at chunk c ^ (l & 7).  With that layout the transform's
+// stages are free of bank conflicts when the span-16 stages put the 16 butterflies j of one row on
+// a half-warp and the span-1 pass moves 16-byte pairs with 8 rows per quarter-warp.  The
+// arithmetic is that of dif_op_dit with radix 16 (the same operations in the same order).
+__device__ __forceinline__ int xsw_offset(int x, int l) {   // byte offset of element (row l, x)
+    return ((x >> 4) << 11) + (l << 7) + ((((x & 15) >> 1) ^ (l & 7)) << 4) + ((x & 1) << 3);
+}
+
+template <int NTHR>
+__device__ __forceinline__ void x16_span16(unsigned char* buf, Twiddles tw, int tid, bool inverse) {
+    // 16 rows x 16 butterflies j, j fastest
+    for (int item = tid; item < 256; item += NTHR) {
+        const int j = item & 15, l = item >> 4;
+        float2 v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = *reinterpret_cast<const float2*>(buf + xsw_offset(j + 16 * q, l));
+        const float2* t = tw.w + j;   // stage L = 256 of the staged W_256 table starts at 0
+        if (!inverse) {
+            dft<16, false>(v);
+#pragma unroll
+            for (int k = 1; k < 16; k++) v[k] = cmul(v[k], t[(k - 1) * 16]);
+        } else {
+            const float* te = tw.e + j;
+#pragma unroll
+            for (int k = 1; k < 16; k++) {
+                const float2 u = cmulc(v[k], t[(k - 1) * 16]);
+                const float e = te[(k - 1) * 16];
+                v[k] = make_float2(fmaf(u.x, e, u.x), fmaf(u.y, e, u.y));
+            }
+            dft<16, true>(v);
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) *reinterpret_cast<float2*>(buf + xsw_offset(j + 16 * q, l)) = v[q];
+    }
+}
+
+template <int NTHR>
+__device__ __forceinline__ void x16_middle(unsigned char* buf, const float4* __restrict__ Rx, int tid) {
+    // the span-1 forward stage, the Rx factors and the span-1 inverse stage, on 16 consecutive
+    // x of one row; rows fastest (8 rows per quarter-warp), pairs of complex per 16-byte access
+    for (int item = tid; item < 256; item += NTHR) {
+        const int l = item & 15, b = item >> 4;
+        unsigned char* row = buf + (b << 11) + (l << 7);
+        float2 v[16];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float4 f = *reinterpret_cast<const float4*>(row + ((c ^ (l & 7)) << 4));
+            v[2 * c] = make_float2(f.x, f.y);
+            v[2 * c + 1] = make_float2(f.z, f.w);
+        }
+        dft<16, false>(v);
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = cmul_df(v[q], __ldg(&Rx[16 * b + q]));
+        dft<16, true>(v);
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            *reinterpret_cast<float4*>(row + ((c ^ (l & 7)) << 4)) = make_float4(v[2 * c].x, v[2 * c].y, v[2 * c + 1].x,
+                                                                                   v[2 * c + 1].y);
+    }
+}
+
+// IFFT_x Rx FFT_x on the 16 rows of a swizzled unit; ends with a CTA barrier
+template <int NTHR>
+__device__ __forceinline__ void x16_linear(unsigned char* buf, Twiddles tw, const float4* Rx, int tid) {
+    x16_span16<NTHR>(buf, tw, tid, false);
+    __syncthreads();
+    x16_middle<NTHR>(buf, Rx, tid);
+    __syncthreads();
+    x16_span16<NTHR>(buf, tw, tid, true);
+    __syncthreads();
+}
+
+template <int NY, int NTHR, int NBUF>
+__global__ void __launch_bounds__(NTHR, 512 / NTHR)
+    plane_x_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, PlaneArgs a,
+                       unsigned int* err) {
+    constexpr int NX = 256, RYS = 16, UNIT_BYTES = RYS * NX * 8;
+    extern __shared__ __align__(1024) unsigned char smem_dyn[];
+    // unit buffers on a 1024-byte boundary of the shared window, where the 128-byte swizzle's
+    // pattern starts (the launch adds 1 KB of slack)
+    unsigned char* smem_raw = smem_dyn + ((1024u - (smem_addr(smem_dyn) & 1023u)) & 1023u);
+    unsigned char* tw_mem = smem_raw + NBUF * UNIT_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tw_mem + ((twiddle_bytes(NX) + 15) / 16) * 16);
+    int& s_arrived = *reinterpret_cast<int*>(bars + NBUF);
+    const int tid = threadIdx.x;
+    constexpr int STRIPS = NY / RYS;
+    const int units = a.Nt * STRIPS;
+    const int nmine = blockIdx.x < units ? (units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int b = 0; b < NBUF; b++) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+    }
+    stage_twiddles<NX, NTHR>(tw_mem, a.twx, tid);
+    const Twiddles tw = Twiddles::packed(tw_mem, NX);
+    __syncthreads();
+    auto buf = [&](int k) { return smem_raw + (k % NBUF) * UNIT_BYTES; };
+    auto coords = [&](int k, int* row0) {
+        const int unit = (int)blockIdx.x + k * (int)gridDim.x;
+        const int slot = unit / STRIPS, y0 = (unit - slot * STRIPS) * RYS;
+        *row0 = slot * NY + y0;
+        return y0;
+    };
+    auto issue = [&](int k) {   // load my k-th unit: 16 boxes
+        int row0;
+        coords(k, &row0);
+        mbar_arrive_expect_tx(&bars[k % NBUF], UNIT_BYTES);
+#pragma unroll 1
+        for (int b = 0; b < NX / 16; b++) tma_load_2d(buf(k) + b * 2048, &tin, 32 * b, row0, &bars[k % NBUF]);
+    };
+    if (tid == 0)
+        for (int k = 0; k < NBUF - 1 && k < nmine; k++) issue(k);
+    for (int k = 0; k < nmine; k++) {
+        int row0;
+        const int y0 = coords(k, &row0);
+        if (tid == 0) s_arrived = mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1)) ? 1 : 0;
+        __syncthreads();
+        if (!s_arrived) {
+            if (tid == 0) {
+                atomicExch(err, KERR_TMA_TIMEOUT);
+                for (int j = k + 1; j < k + NBUF - 1 && j < nmine; j++) mbar_wait(&bars[j % NBUF], (uint32_t)((j / NBUF) & 1));
+                bulk_wait<0>();
+            }
+            return;
+        }
+        mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1));   // completed: returns at once
+        unsigned char* u = buf(k);
+        x16_linear<NTHR>(u, tw, a.t1.Rx, tid);
+        if (a.lens) {
+            for (int e = tid; e < RYS * NX; e += NTHR) {
+                const int x = e % NX, r = e / NX;
+                float2* pe = reinterpret_cast<float2*>(u + xsw_offset(x, r));
+                *pe = cmul(*pe, cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y0 + r])));
+            }
+            __syncthreads();
+            x16_linear<NTHR>(u, tw, a.t2.Rx, tid);
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll 1
+            for (int b = 0; b < NX / 16; b++) tma_store_2d(&tout, 32 * b, row0, u + b * 2048);
+            bulk_commit();
+            if (k + NBUF - 1 < nmine) {
+                bulk_wait_read<1>();   // the previous unit's stores have left its buffer
+                issue(k + NBUF - 1);
+            }
+        }
+    }
+    if (tid == 0) bulk_wait<0>();
 }
 
 // x part: units are (slot, strip of RYS rows); with the mirror lens, x(t1), the lens, x(t2).

@@ -11,18 +11,57 @@
 //   PL           plane passes: 1, one cluster kernel per sweep (plane_kernel); 2, the y part on
 //                column strips and the x part on row strips, two kernels over HBM without
 //                clusters (plane_y_kernel, plane_x_kernel), one more pass over HBM but every SM
-//                busy and no cluster barrier (the faster choice on every grid measured);
+//                busy and no cluster barrier; 3, as 2 with the y part staged by TMA bulk tensor
+//                copies (plane_y_tma_kernel: persistent 256-thread CTAs, 3 unit buffers each);
+//                4, both parts staged by TMA (plane_x_tma_kernel for the x part, Nx = 256);
 //   plane unit   PT threads per CTA and 512 / PT CTAs per SM, each CTA holding a
 //                PLB = 128 KB * PT / 512 share of the unit; PL = 1: SLO == 2, the two interleaved
 //                omega-planes split over CL CTAs; SLO == 1, planes larger than PLB split over
 //                CL CTAs, smaller planes batched PB per CTA; PL = 2: strips of PLB bytes.
 // Several variants of one grid may be compiled in; they differ only in speed.
 #pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <mutex>
 
 #include "mpc_kernels.cuh"
 
 namespace mpc {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda)
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The field (complex64, slot layout SLO = 1) as a 2-D FLOAT32 tensor of rows of 2 Nx floats,
+// Ny * Nt rows, with boxes of box_x floats by box_rows rows.
+inline cudaError_t field_tensor_map(CUtensorMap* m, const void* field, int Nx, long rows, int box_x, int box_rows,
+                                    CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)(2 * Nx), (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(2 * Nx) * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(field), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
 
 struct ShapeOps {
     int Nx, Ny, Nt, P, SLO, CL, PB, PT, CH, LD, PL;
@@ -41,14 +80,19 @@ struct Shape {
     static constexpr int SLO = SLO_ > 0 ? SLO_ : ((P < 16) ? 16 / P : 1);
     static constexpr long PLANE_B = (long)NX * NY * 8;
     static constexpr long PLB = 131072L * PT / kThreads;
-    static constexpr int CL = PL == 2 ? 1
+    static constexpr int CL = PL >= 2 ? 1
                               : (SLO == 2) ? (int)(PLANE_B * 2 / PLB) : (PLANE_B > PLB ? (int)(PLANE_B / PLB) : 1);
-    static constexpr int PB = PL == 2 ? 1
+    static constexpr int PB = PL >= 2 ? 1
                               : (SLO == 2) ? 2 : (PLANE_B > PLB ? 1 : ((PLB / PLANE_B) < NT ? (int)(PLB / PLANE_B) : NT));
     // PL = 2: column strips of CXS columns and row strips of RYS rows, PLB bytes each
     static constexpr int CXS = (int)(PLB / (NY * 8L)), RYS = (int)(PLB / (NX * 8L));
-    static_assert(PL == 1 || (PL == 2 && SLO == 1 && CXS >= 2 && CXS <= NX && RYS >= 1 && RYS <= NY),
+    static_assert(PL == 1 || (PL >= 2 && PL <= 4 && SLO == 1 && CXS >= 2 && CXS <= NX && RYS >= 1 && RYS <= NY),
                   "two-pass planes: SLO 1, strips within the plane");
+    // PL = 3: the TMA-staged y pass on 16-column strips (128 B box rows), 256 threads, 3 buffers
+    static constexpr int TCX = 16, TTH = 256, TNB = 3;
+    static_assert(PL < 3 || (NX % TCX == 0 && NY <= 256), "TMA boxes: 16 columns, at most 256 rows");
+    static_assert(PL != 4 || (NX == 256 && NY % 16 == 0), "TMA x part: rows of 256, strips of 16 rows");
+    static constexpr int XSMEM = 1024 + 3 * 32768 + ((twiddle_bytes(256) + 15) / 16) * 16 + 3 * 8 + 16;
     static_assert(SLO == 1 || SLO == 2, "slot interleave");
     static_assert(PT == 128 || PT == 256 || PT == 512, "plane threads");
     static_assert(P >= 4 && P <= NX * NY, "pencil tile must fit the grid");
@@ -69,7 +113,30 @@ struct Shape {
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_EXIT_C64, CH, LD>), PC::smem(PM_EXIT_C64));
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_TEMP, CH, LD>), PC::smem(PM_TEMP));
         MPC_SET_SMEM((pencil_kernel<NT, P, SLO, PM_IONIZ, CH, LD>), PC::smem(PM_IONIZ));
-        if constexpr (PL == 2) {
+        if constexpr (PL >= 2) {
+            if constexpr (PL == 4) {
+                MPC_SET_SMEM((plane_x_tma_kernel<NY, TTH, TNB>), XSMEM);
+                int dev1 = 0, nsm1 = 0, bx1 = 0;
+                if ((e = cudaGetDevice(&dev1)) != cudaSuccess) return e;
+                if ((e = cudaDeviceGetAttribute(&nsm1, cudaDevAttrMultiProcessorCount, dev1)) != cudaSuccess) return e;
+                if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx1, plane_x_tma_kernel<NY, TTH, TNB>, TTH, XSMEM)) !=
+                    cudaSuccess)
+                    return e;
+                if (bx1 <= 0) return cudaErrorInvalidConfiguration;
+                tma_grid_x = bx1 * nsm1 < NT * (NY / 16) ? bx1 * nsm1 : NT * (NY / 16);
+            }
+            if constexpr (PL >= 3) {
+                if (!tensor_map_encoder()) return cudaErrorNotSupported;
+                MPC_SET_SMEM((plane_y_tma_kernel<NX, NY, TCX, TTH, TNB>), (StripYTmaCfg<NX, NY, TCX>::SMEM(TNB)));
+                int dev0 = 0, nsm0 = 0, bt = 0;
+                if ((e = cudaGetDevice(&dev0)) != cudaSuccess) return e;
+                if ((e = cudaDeviceGetAttribute(&nsm0, cudaDevAttrMultiProcessorCount, dev0)) != cudaSuccess) return e;
+                if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, plane_y_tma_kernel<NX, NY, TCX, TTH, TNB>, TTH,
+                                                                       StripYTmaCfg<NX, NY, TCX>::SMEM(TNB))) != cudaSuccess)
+                    return e;
+                if (bt <= 0) return cudaErrorInvalidConfiguration;
+                tma_grid_y = bt * nsm0 < NT * (NX / TCX) ? bt * nsm0 : NT * (NX / TCX);
+            }
             MPC_SET_SMEM((plane_y_kernel<NX, NY, CXS, PT, PMB>), (StripYCfg<NX, NY, CXS>::SMEM));
             MPC_SET_SMEM((plane_x_kernel<NX, NY, RYS, PT, PMB>), (StripXCfg<NX, NY, RYS>::SMEM));
             int dev = 0, nsm = 0, by = 0, bx = 0;
@@ -110,11 +177,52 @@ struct Shape {
         return cudaGetLastError();
     }
 
-    // PL = 2: resident-CTA grids of the two strip kernels (set by setup)
-    static inline int strip_grid_y = 0, strip_grid_x = 0;
+    // PL = 2, 3: resident-CTA grids of the strip kernels (set by setup)
+    static inline int strip_grid_y = 0, strip_grid_x = 0, tma_grid_y = 0, tma_grid_x = 0;
+
+    // the TMA-staged y pass from `in` to `out` (tensor maps encoded per launch: a few host
+    // microseconds, no device work)
+    static cudaError_t plane_y_tma(const PlaneArgs& a, int second, cudaStream_t st) {
+        CUtensorMap tin, tout;
+        cudaError_t e;
+        if ((e = field_tensor_map(&tin, a.in, NX, (long)NY * NT, 2 * TCX, NY)) != cudaSuccess) return e;
+        if ((e = field_tensor_map(&tout, a.out, NX, (long)NY * NT, 2 * TCX, NY)) != cudaSuccess) return e;
+        plane_y_tma_kernel<NX, NY, TCX, TTH, TNB><<<tma_grid_y, TTH, StripYTmaCfg<NX, NY, TCX>::SMEM(TNB), st>>>(
+            tin, tout, a, second, a.err);
+        return cudaGetLastError();
+    }
+
+    // the TMA-staged x pass, in place on a.out (row strips of 16 rows, 16 swizzled boxes each)
+    static cudaError_t plane_x_tma(const PlaneArgs& a, cudaStream_t st) {
+        CUtensorMap tin, tout;
+        cudaError_t e;
+        if ((e = field_tensor_map(&tin, a.in, NX, (long)NY * NT, 32, 16, CU_TENSOR_MAP_SWIZZLE_128B)) != cudaSuccess)
+            return e;
+        if ((e = field_tensor_map(&tout, a.out, NX, (long)NY * NT, 32, 16, CU_TENSOR_MAP_SWIZZLE_128B)) != cudaSuccess)
+            return e;
+        if constexpr (PL == 4) plane_x_tma_kernel<NY, TTH, TNB><<<tma_grid_x, TTH, XSMEM, st>>>(tin, tout, a, a.err);
+        return cudaGetLastError();
+    }
 
     static cudaError_t plane(const PlaneArgs& a, int nclusters, cudaStream_t st) {
-        if constexpr (PL == 2) {
+        if constexpr (PL == 4) {
+            PlaneArgs b = a;
+            b.in = a.out;   // the passes after the first run in place
+            cudaError_t e;
+            if ((e = plane_y_tma(a, 0, st)) != cudaSuccess) return e;
+            if ((e = plane_x_tma(b, st)) != cudaSuccess) return e;
+            if (a.lens) return plane_y_tma(b, 1, st);
+            return cudaSuccess;
+        } else if constexpr (PL == 3) {
+            PlaneArgs b = a;
+            b.in = a.out;   // the passes after the first run in place
+            cudaError_t e;
+            if ((e = plane_y_tma(a, 0, st)) != cudaSuccess) return e;
+            plane_x_kernel<NX, NY, RYS, PT, PMB><<<strip_grid_x, PT, StripXCfg<NX, NY, RYS>::SMEM, st>>>(b);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if (a.lens) return plane_y_tma(b, 1, st);
+            return cudaSuccess;
+        } else if constexpr (PL == 2) {
             PlaneArgs b = a;
             b.in = a.out;   // the passes after the first run in place
             plane_y_kernel<NX, NY, CXS, PT, PMB><<<strip_grid_y, PT, StripYCfg<NX, NY, CXS>::SMEM, st>>>(a, 0);
@@ -139,7 +247,7 @@ struct Shape {
     }
 
     static int max_clusters() {
-        if constexpr (PL == 2) {
+        if constexpr (PL >= 2) {
             return strip_grid_y;   // CTAs of the y pass (clusters of one)
         } else {
             cudaLaunchConfig_t cfg = {};
@@ -168,7 +276,7 @@ struct Shape {
     }
 
     static constexpr int plane_smem() {
-        if constexpr (PL == 2) return StripYCfg<NX, NY, CXS>::SMEM;
+        if constexpr (PL >= 2) return StripYCfg<NX, NY, CXS>::SMEM;
         else return LC::SMEM;
     }
 

@@ -16,5 +16,7 @@ const ShapeOps* const shape_list_c[] = {
     Shape<256,256,2048,1,256,16384,16>::ops(),     // SLO 1, 1024-thread pencil CTAs (16-sample chunks)
     Shape<256,256,2048,1,256,8192,32,0,2>::ops(),  // 4-pencil tiles, two-pass plane on 32-wide strips
     Shape<256,256,2048,1,128,8192,32,0,2,5>::ops(),  // as variant 0, strip kernels at five CTAs per SM
+    Shape<256,256,2048,1,128,8192,32,0,3>::ops(),  // as variant 0, the y pass staged by TMA
+    Shape<256,256,2048,1,128,8192,32,0,4>::ops(),  // as variant 0, both strip passes staged by TMA
     nullptr};
 }  // namespace mpc

@@ -59,6 +59,7 @@ struct or64_ctx {
     double2* tab = nullptr;      // expD0 (Nt), expRx (Nx), expRy (Ny)
     double* wbuff = nullptr;     // fftshift(w), Nt
     double* red = nullptr;       // reductions: 2 sums + per-pencil energies (NP)
+    double* W = nullptr;         // ionization terms, 5 N (plasma on; allocated on first use)
     std::vector<double> henergy;
     // ionization constants (plasma.c:118-213)
     double Kon, I1, Kon1, Kon2, Kon3, Kon4, Kon5, Kon6, K1, K2, K3, K4, K5;
@@ -105,16 +106,57 @@ struct NLArgs {
     long NP;
 };
 
-// The nonlinear step of one (x, y) pencil per thread, along t: or_sst's combination
-// (propagation.c:215-233), or_ioniz (plasma.c:118-245, corrected, run forward in t), the
-// combine (propagation.c:283-309) and the apply (propagation.c:315-327).  d holds the
-// unnormalised IFFT_t of -i w FFT_t A (sst_on) and is not used otherwise.
-__global__ void k_nonlinear(double2* A, const double2* d, NLArgs a) {
+// The nonlinear step (propagation.c:164-327, plasma.c:118-245, corrected, the prefix run forward
+// in t) in three passes with the CPU oracle's operations in its order: the per-point ionization
+// terms (every point in parallel), the prefix along t (one pencil per thread), then the combine
+// and the apply (every point in parallel).  d holds the unnormalised IFFT_t of -i w FFT_t A
+// (sst_on) and is not read otherwise.
+// W[0] = W1 (then fe_sp), W[1] = W2, W[2] = Wava, W[3] = sigma, W[4] = tau_c; N values each.
+__global__ void k_ion_terms(const double2* A, NLArgs a, long N, double* W) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
+        const double2 Aq = A[q];
+        const double absA = hypot(Aq.x, Aq.y);
+        double Ip = pow(absA, 2) * HBAR * a.w0;                      // plasma.c:133-139
+        if (Ip == 0) Ip = 1e-30;
+        const double E0 = sqrt(2.0 * ZW0 * Ip / NC) * FCTR;          // :145-149
+        const double dat = fabs(E0) / EF;
+        double r1 = a.Kon1 * pow(a.Kon3 / dat, a.Kon5) * exp(-a.Kon3 / (3.0 * dat));
+        double r2 = a.Kon2 * pow(a.Kon4 / dat, a.Kon6) * exp(-a.Kon4 / (3.0 * dat));
+        if (isnan(r1)) r1 = 0.0;                                      // :184-192
+        if (isnan(r2)) r2 = 0.0;
+        const double ve = sqrt(a.K1 * pow(E0, 2.0) / (a.K2 * pow(0.0 + a.w0, 2.0)));   // A18
+        const double tc = 1.0 / (a.K3 * ve);                          // :203-213
+        const double sg = isinf(tc) ? 0.0 : a.K4 * tc / (1.0 + a.K5 * pow(tc, 2.0));  // A27
+        W[q] = r1;
+        W[N + q] = r2;
+        W[2 * N + q] = sg * Ip / a.I1;
+        W[3 * N + q] = sg;
+        W[4 * N + q] = tc;
+    }
+}
+
+// the prefix along t of one pencil per thread (plasma.c:223-231 forward, :238-241): W[0] := fe_sp
+__global__ void k_ion_prefix(NLArgs a, long N, double* W) {
     const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (i >= a.NP) return;
     double R = 0.0, ions1 = 0.0, ions2 = 0.0;   // ions1[k], ions2[k] before slice k
     for (int k = 0; k < a.Nt; k++) {
         const long q = (long)k * a.NP + i;
+        const double W1 = W[q], W2 = W[N + q], Wava = W[2 * N + q], sg = W[3 * N + q];
+        W[q] = (ions1 * 1.0 + ions2 * 2.0) * sg;
+        R = R + W1 * a.Kon;
+        R = R + (1.0 - R) * Wava * a.Kon;
+        const double n1 = 1.0 - exp(-R) - ions2;
+        const double n2 = ions2 + W2 * a.Kon * ions1;
+        ions1 = n1;
+        ions2 = n2;
+    }
+}
+
+// the combine (propagation.c:283-309, A13) and the apply (:317-327, A14); W is read only with
+// plasma on
+__global__ void k_nl_apply(double2* A, const double2* d, NLArgs a, long N, const double* W) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
         const double2 Aq = A[q];
         double sre = 0.0, sim = 0.0;
         if (a.sst_on == 1) {
@@ -130,36 +172,17 @@ __global__ void k_nonlinear(double2* A, const double2* d, NLArgs a) {
         const double absA = hypot(Aq.x, Aq.y);
         double anr, ani;
         if (a.plasm == 1) {
-            double Ip = pow(absA, 2) * HBAR * a.w0;                      // plasma.c:133-139
-            if (Ip == 0) Ip = 1e-30;
-            const double E0 = sqrt(2.0 * ZW0 * Ip / NC) * FCTR;          // :145-149
-            const double dat = fabs(E0) / EF;
-            double r1 = a.Kon1 * pow(a.Kon3 / dat, a.Kon5) * exp(-a.Kon3 / (3.0 * dat));
-            double r2 = a.Kon2 * pow(a.Kon4 / dat, a.Kon6) * exp(-a.Kon4 / (3.0 * dat));
-            if (isnan(r1)) r1 = 0.0;                                      // :184-192
-            if (isnan(r2)) r2 = 0.0;
-            const double ve = sqrt(a.K1 * pow(E0, 2.0) / (a.K2 * pow(0.0 + a.w0, 2.0)));   // A18
-            const double tc = 1.0 / (a.K3 * ve);                          // :203-213
-            const double sg = isinf(tc) ? 0.0 : a.K4 * tc / (1.0 + a.K5 * pow(tc, 2.0));  // A27
-            const double Wava = sg * Ip / a.I1;
-            const double fe = (ions1 * 1.0 + ions2 * 2.0) * sg;          // :238-241
-            R = R + r1 * a.Kon;                                           // :223-231, forward
-            R = R + (1.0 - R) * Wava * a.Kon;
-            const double n1 = 1.0 - exp(-R) - ions2;
-            const double n2 = ions2 + r2 * a.Kon * ions1;
-            ions1 = n1;
-            ions2 = n2;
-            const double z1 = a.gamma2 * pow(absA, 2.0);                  // propagation.c:283-293 (A13)
-            const double pl = a.rho_nt * fe / 2.0;
-            const double z2y = a.w0 * tc * pl;
+            const double z1 = a.gamma2 * pow(absA, 2.0);
+            const double pl = a.rho_nt * W[q] / 2.0;
+            const double z2y = a.w0 * W[4 * N + q] * pl;
             anr = (0.0 - sre - pl);
             ani = (z1 - sim - z2y);
         } else {
-            const double tempab = pow(absA, 2.0);                         // :303-309
+            const double tempab = pow(absA, 2.0);
             anr = -sre;
             ani = a.gamma2 * tempab - sim;
         }
-        const double er = exp(a.dzz * anr);                               // :317-327 (A14)
+        const double er = exp(a.dzz * anr);
         const double ei = a.dzz * ani;
         const double c = cos(ei), s = sin(ei);
         const double nx = Aq.x * er * c - Aq.y * er * s;
@@ -309,7 +332,7 @@ static int beam_profiles(or64_ctx* c, const double2* A, double* BP1, double* BP2
 }
 
 // The nonlinear step of propagation.c:164-327 on device field A: the SST derivative
-// (t transforms, -i w) and k_nonlinear.
+// (t transforms, -i w) and the three nonlinear passes.
 static int nonlinear(or64_ctx* c, double2* A, double dzz) {
     const or_params* p = &c->p;
     if (p->sst_on == 1) {
@@ -333,8 +356,15 @@ static int nonlinear(or64_ctx* c, double2* A, double dzz) {
     a.plasm = p->plasm;
     a.Nt = c->Nt;
     a.NP = c->NP;
-    k_nonlinear<<<(int)((c->NP + 127) / 128), 128, 0, c->st>>>(A, c->buf, a);
-    CK(cudaGetLastError(), "k_nonlinear");
+    if (p->plasm == 1) {
+        if (!c->W) CK(cudaMalloc(&c->W, sizeof(double) * 5 * c->N), "cudaMalloc ionization terms");
+        k_ion_terms<<<grid_for(c->N), 256, 0, c->st>>>(A, a, c->N, c->W);
+        CK(cudaGetLastError(), "k_ion_terms");
+        k_ion_prefix<<<(int)((c->NP + 127) / 128), 128, 0, c->st>>>(a, c->N, c->W);
+        CK(cudaGetLastError(), "k_ion_prefix");
+    }
+    k_nl_apply<<<grid_for(c->N), 256, 0, c->st>>>(A, c->buf, a, c->N, c->W);
+    CK(cudaGetLastError(), "k_nl_apply");
     return 0;
 }
 
@@ -382,7 +412,7 @@ int or64_destroy(or64_ctx* c) {
     if (c->plan3) cufftDestroy(c->plan3);
     if (c->plant) cufftDestroy(c->plant);
     for (void* ptr : {(void*)c->A, (void*)c->C1, (void*)c->C2, (void*)c->buf, (void*)c->tab, (void*)c->wbuff,
-                      (void*)c->red})
+                      (void*)c->red, (void*)c->W})
         if (ptr) cudaFree(ptr);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;

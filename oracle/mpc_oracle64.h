@@ -24,8 +24,9 @@ typedef struct or64_ctx or64_ctx;
 
 const char *or64_last_error(void);
 
-/* A context on the current device: the field and the three work fields C1, C2 and the
- * derivative buffer (4 x 16 N bytes), the cuFFT plans and the tables.  Returns 0 or -1. */
+/* A context on the current device: the field, the derivative buffer, the two step-doubling
+ * fields C1, C2 (allocated on the first attempt) and the ionization terms (5 x 8 N bytes, on
+ * the first step with plasma), the cuFFT plans and the tables.  Returns 0 or -1. */
 int or64_create(or64_ctx **out, const or_params *p, const or_switches *sw);
 int or64_destroy(or64_ctx *c);
 

@@ -24,10 +24,27 @@ def test_fft_flop_count(bench):
 
 
 def test_profile_traffic_from_committed_summary(bench):
-    t = bench.profile_traffic("pencil_step_256x256x2048.txt")
     algorithmic = 16 * 256 * 256 * 2048
+    wl = bench.WORKLOADS["cell256"]["profile"]
+    t = bench.profile_traffic(wl["pencil"])
     assert t is not None and 0.9 * algorithmic < t < 1.2 * algorithmic
-    assert bench.profile_traffic("no_such_summary.txt") is None
+    # the plane sweep's two kernels, summed: two passes over the field
+    t2 = bench.profile_traffic(wl["plane"])
+    assert t2 is not None and 1.8 * algorithmic < t2 < 2.4 * algorithmic
+    assert bench.profile_traffic(["no_such_summary.txt"]) is None
+    assert bench.profile_traffic(["pencil_step_256x256x2048.txt", "no_such_summary.txt"]) is None
+
+
+def test_whole_run_accuracy_reader(bench, tmp_path, monkeypatch):
+    class P:
+        Nx, Ny, Nt = 8, 8, 16
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.whole_run_accuracy(P()) is None
+    (tmp_path / "profiles").mkdir()
+    (tmp_path / "profiles" / "accuracy_whole_run_8x8x16.txt").write_text(
+        "command: x\nsplit_steps: 3200\nfield_rel_l2: 4.5e-05\nspectrum_rel_l2: 2e-05\nenergy_drift: 1e-6\n")
+    r = bench.whole_run_accuracy(P())
+    assert r["split_steps"] == 3200 and r["field_rel_l2"] == 4.5e-05 and r["energy_drift"] == 1e-6
 
 
 def test_workloads_name_existing_cells(bench):

@@ -145,7 +145,7 @@ def _shape_cfg(NX, NY, NT, SLO_=0, PT=512, TP=16384, CH=32, LD=1, PL=1, PMB=0):
     SLO = SLO_ if SLO_ > 0 else (16 // P if P < 16 else 1)
     plane_b = NX * NY * 8
     plb = 131072 * PT // 512
-    if PL == 2:
+    if PL >= 2:
         CL, PB = 1, 1
     elif SLO == 2:
         CL, PB = plane_b * 2 // plb, 2
@@ -177,9 +177,11 @@ def _views(*variant):
         pl, xl = divmod(l, CX)
         return (y // RY) * RSZ + (pl * RY + (y % RY)) * RS + xl
 
-    if variant[8] == 2:   # two-pass plane: column strips (line = column) and row strips (line = row)
+    if variant[8] in (2, 3):   # two-pass plane: column strips (line = column) and row strips (line = row)
         plb = 131072 * variant[4] // 512
         CXS, RYS = plb // (NY * 8), plb // (NX * 8)
+        if variant[8] >= 3:    # the y pass staged by TMA: 16-column strips, 256 threads
+            CXS = 16
         return [("pencil", NT, P, pen, psize), ("strip_y", NY, CXS, lambda y, l: y * CXS + l, NY * CXS),
                 ("strip_x", NX, RYS, lambda x, l: l * (NX + 1) + x, RYS * (NX + 1))]
     return [("pencil", NT, P, pen, psize), ("row", NX, PB * RY, row, CL * RSZ), ("col", NY, PB * CX, col, CL * RSZ)]
@@ -189,6 +191,7 @@ def test_variant_list_parsed():
     assert (256, 256, 2048, 0, 512, 16384, 32, 1, 1, 0) in SHAPES and (256, 256, 2048, 1, 256, 16384, 16, 1, 1, 0) in SHAPES
     assert (256, 256, 2048, 1, 256, 8192, 32, 0, 1, 0) in SHAPES and (512, 512, 1024, 1, 256, 16384, 32, 1, 2, 0) in SHAPES
     assert (256, 256, 2048, 1, 128, 8192, 32, 0, 2, 5) in SHAPES
+    assert (256, 256, 2048, 1, 128, 8192, 32, 0, 3, 0) in SHAPES
     assert len({v[:3] for v in SHAPES}) >= 7
 
 
@@ -225,7 +228,45 @@ def test_pencil_view_bank_conflict_free(shape):
             assert _wavefronts([at(CH * (t // P) + i, t % P) for t in range(w0, w0 + 32)]) <= 2, (shape, i)
 
 
-@pytest.mark.parametrize("shape", [v for v in SHAPES if v[8] == 2])
+def _xsw(x, l):
+    """Byte offset of element (row l, x) in the TMA x pass's swizzled unit (mpc_kernels.cuh xsw_offset)."""
+    return ((x >> 4) << 11) + (l << 7) + ((((x & 15) >> 1) ^ (l & 7)) << 4) + ((x & 1) << 3)
+
+
+def _wavefronts_bytes(accesses):
+    """Wavefronts of one warp-wide access given (thread, byte offset, width): threads are served
+    128 bytes at a time (half-warps for 8-byte, quarter-warps for 16-byte accesses); within a
+    phase every distinct 4-byte word of a bank costs one wavefront."""
+    width = accesses[0][2]
+    per = 128 // width
+    total = 0
+    for g in range(0, len(accesses), per):
+        banks = {}
+        for _, off, w in accesses[g:g + per]:
+            for wd in range(off // 4, (off + w) // 4):
+                banks.setdefault(wd % 32, set()).add(wd)
+        total += max(len(v) for v in banks.values())
+    return total
+
+
+def test_tma_x_swizzle_is_a_permutation_and_conflict_free():
+    """The TMA x pass's unit layout (16 boxes of 16 rows x 128 B with the 128-byte swizzle) covers
+    the 32 KB unit once, and its three passes over a unit take the minimum wavefronts per warp
+    access: the span-16 stages (8-byte accesses, 16 butterflies j of a row per half-warp) and
+    the span-1 pass (16-byte pairs, 8 rows per quarter-warp)."""
+    offs = sorted(_xsw(x, l) for l in range(16) for x in range(256))
+    assert offs == list(range(0, 32768, 8))
+    for w0 in range(0, 256, 32):               # span-16 stages: item -> (j = item & 15, l = item >> 4)
+        for q in range(16):
+            acc = [(t, _xsw((t & 15) + 16 * q, t >> 4), 8) for t in range(w0, w0 + 32)]
+            assert _wavefronts_bytes(acc) == 2, (w0, q)
+    for w0 in range(0, 256, 32):               # span-1 pass: item -> (l = item & 15, b = item >> 4)
+        for c in range(8):
+            acc = [(t, (((t >> 4) << 11) + ((t & 15) << 7) + ((c ^ ((t & 15) & 7)) << 4)), 16) for t in range(w0, w0 + 32)]
+            assert _wavefronts_bytes(acc) == 4, (w0, c)
+
+
+@pytest.mark.parametrize("shape", [v for v in SHAPES if v[8] in (2, 3, 4)])
 def test_strip_views_bank_conflict_free(shape):
     """The two-pass plane's strip views: every FFT stage (lines fastest across a warp, as the
     stage loops take them) reads and writes with the minimum two wavefronts per warp access."""
