@@ -186,12 +186,14 @@ int mpc_mlp_predict(mpc_mlp *mlp, const float *X, int n, float *y);
 /* One sample, without allocating (the controller's per-step call). */
 int mpc_mlp_predict1(mpc_mlp *mlp, const float x[MPC_NFEATURES], float *y);
 
-/* The learned controller (run to state.z = dist): plain split steps (mpc_step) of
+/* The learned controller (run to state.z = dist): plain split steps (mpc_step's arithmetic) of
  * dz = safety * Cav * exp(network(features)), capped at twice the previous step, quantised
- * down to 16 steps per octave of Cav and shortened to land on the next mirror plane; the run opens with one step-doubling attempt, and every
- * check_every steps the step is taken as a step-doubling attempt instead, whose error checks
- * the network: above def_err, the next fallback_len accepted steps are plain step doubling
- * (mpc_step_double) before the network is used again. */
+ * down to 16 steps per octave of Cav and shortened to land on the next mirror plane; the run
+ * opens with one step-doubling attempt, and every check_every steps the step is taken as a
+ * step-doubling attempt instead, whose error checks the network: above def_err, the next
+ * fallback_len accepted steps are plain step doubling (mpc_step_double) before the network is
+ * used again.  Consecutive plain steps share one plane sweep (the second linear half step of one
+ * and the first of the next, as mpc_run_fixed does). */
 typedef struct {
     int steps;              /* plain steps at the network's dz */
     int checks;             /* periodic step-doubling checks */
@@ -202,6 +204,10 @@ typedef struct {
 } mpc_learned_stats;
 int mpc_run_learned(mpc_ctx *ctx, mpc_mlp *mlp, double safety, int check_every, int fallback_len,
                     mpc_learned_stats *out);
+/* As mpc_run_learned, with one prediction (feature pass, network call) held for `hold`
+ * consecutive plain steps (no counterpart in the reference; mpc_run_learned is hold = 1). */
+int mpc_run_learned_hold(mpc_ctx *ctx, mpc_mlp *mlp, double safety, int check_every, int fallback_len, int hold,
+                         mpc_learned_stats *out);
 
 /* One mirror bounce of the device-resident field, now: MPC_BOUNCE_LENS multiplies it by the
  * mirror's focusing phase exp(-i k0 (x^2 + y^2) / roc); MPC_BOUNCE_SIGNFLIP flips

@@ -96,6 +96,7 @@ SIGNATURES = {
     "mpc_mlp_predict": (C.c_int, [C.c_void_p, _fp, C.c_int, _fp]),
     "mpc_mlp_predict1": (C.c_int, [C.c_void_p, _fp, _fp]),
     "mpc_run_learned": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_void_p]),
+    "mpc_run_learned_hold": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_void_p]),
 }
 
 _fp = C.POINTER(C.c_float)
@@ -292,10 +293,11 @@ class Propagator:
         _check(self.lib.mpc_features(self.h, f.ctypes.data_as(_fp)), "mpc_features")
         return f
 
-    def run_learned(self, mlp: "MLP", safety: float = 0.9, check_every: int = 8, fallback_len: int = 4) -> dict:
+    def run_learned(self, mlp: "MLP", safety: float = 0.9, check_every: int = 8, fallback_len: int = 4,
+                    hold: int = 1) -> dict:
         st = c_mpc_learned_stats()
-        _check(self.lib.mpc_run_learned(self.h, mlp.h, float(safety), int(check_every), int(fallback_len), C.byref(st)),
-               "mpc_run_learned")
+        _check(self.lib.mpc_run_learned_hold(self.h, mlp.h, float(safety), int(check_every), int(fallback_len),
+                                             int(hold), C.byref(st)), "mpc_run_learned_hold")
         return {k: getattr(st, k) for k, _ in st._fields_}
 
     def mirror_bounce(self, mode: int) -> None:

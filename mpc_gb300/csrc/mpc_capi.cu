@@ -103,14 +103,18 @@ __device__ __forceinline__ float4 split_df(double2 z) {
 }
 
 // Double-float tables of the plane sweep: Rx_df[px] and RyD_df[y * Nt + pos] = Ry[y] D[pos]
-// (the product formed in FP64).
+// (the product formed in FP64), and the same products slot-major, RyDT_df[pos * Ny + y], so that
+// one slot's Ny factors are contiguous (the TMA-staged y pass copies them in one piece).
 __global__ void k_split(const double2* Rx, const double2* Ry, const double2* D, int Nx, int Ny, int Nt,
-                        float4* Rx_df, float4* RyD_df) {
+                        float4* Rx_df, float4* RyD_df, float4* RyDT_df) {
     const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (i < Nx) Rx_df[i] = split_df(Rx[i]);
     if (i < (long)Ny * Nt) {
-        const double2 a = Ry[i / Nt], b = D[i % Nt];
-        RyD_df[i] = split_df(make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x));
+        const long y = i / Nt, pos = i % Nt;
+        const double2 a = Ry[y], b = D[pos];
+        const float4 f = split_df(make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x));
+        RyD_df[i] = f;
+        RyDT_df[pos * Ny + y] = f;
     }
 }
 
@@ -166,18 +170,31 @@ __global__ void k_diffnorm_c128(const double2* __restrict__ a, const double2* __
     }
 }
 
+// The reductions below add each thread's values in FP32 over runs of kRun elements and the run
+// sums in FP64 (within the thread, then across threads): GB300 issues FP64 at 1/64 of its FP32
+// rate, and an FP64 add per element made these passes FP64-bound instead of HBM-bound.  A run sum
+// of kRun non-negative FP32 terms is within kRun * 2^-24 (relative) of exact.
+constexpr int kRun = 32;
+
 // Richardson combination and error sums of one step-doubling attempt (MPC.c:350-381 and
 // propagation.c:624-633, on the device field): out = (4 C2 - C1) / 3 (out may alias C1),
-// sums[0] += |C2 - C1|^2, sums[1] += |C2|^2, accumulated in FP64.
+// sums[0] += |C2 - C1|^2, sums[1] += |C2|^2.
 __global__ void k_richardson(const float2* C1, const float2* C2, float2* out, long n, double* sums) {
     __shared__ double sh[32];
     double s1 = 0.0, s2 = 0.0;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const float2 a = C1[i], b = C2[i];
-        const float dx = b.x - a.x, dy = b.y - a.y;
-        s1 += (double)fmaf(dx, dx, dy * dy);
-        s2 += (double)fmaf(b.x, b.x, b.y * b.y);
-        out[i] = make_float2(fmaf(4.0f / 3.0f, b.x, -a.x / 3.0f), fmaf(4.0f / 3.0f, b.y, -a.y / 3.0f));
+    const long stride = (long)gridDim.x * blockDim.x;
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    while (i < n) {
+        float p1 = 0.0f, p2 = 0.0f;
+        for (int j = 0; j < kRun && i < n; j++, i += stride) {
+            const float2 a = C1[i], b = C2[i];
+            const float dx = b.x - a.x, dy = b.y - a.y;
+            p1 += fmaf(dx, dx, dy * dy);
+            p2 += fmaf(b.x, b.x, b.y * b.y);
+            out[i] = make_float2(fmaf(4.0f / 3.0f, b.x, -a.x / 3.0f), fmaf(4.0f / 3.0f, b.y, -a.y / 3.0f));
+        }
+        s1 += (double)p1;
+        s2 += (double)p2;
     }
     s1 = block_sum(s1, sh);
     s2 = block_sum(s2, sh);
@@ -192,37 +209,59 @@ __global__ void k_pencil_energy_slots(const float2* __restrict__ S, int NP, int 
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= NP) return;
     double acc = 0.0;
-    for (int s = 0; s < Nt; s++) {
-        const float2 v = S[((size_t)(s / SLO) * NP + q) * SLO + (s % SLO)];
-        acc += (double)fmaf(v.x, v.x, v.y * v.y);
+    for (int s0 = 0; s0 < Nt; s0 += kRun) {
+        float part = 0.0f;
+        const int s1 = s0 + kRun < Nt ? s0 + kRun : Nt;
+        for (int s = s0; s < s1; s++) {
+            const float2 v = S[((size_t)(s / SLO) * NP + q) * SLO + (s % SLO)];
+            part = fmaf(v.x, v.x, fmaf(v.y, v.y, part));
+        }
+        acc += (double)part;
     }
     E[q] = acc * scale;
 }
 
-// Moments of the field S (slot layout) for the step-size features, FP64 across threads:
+// Moments of the field S (slot layout) for the step-size features:
 // out = {sum |S|^2, sum w|S|^2, sum w^2|S|^2, sum x|S|^2, sum x^2|S|^2, sum y|S|^2, sum y^2|S|^2}
-// (w = omega offset of the slot, x, y = transverse positions) and mx = max |S|^2 (bit pattern).
-__global__ void k_moments(const float2* __restrict__ S, long N, int NP, int Nx, int SLO, const float* __restrict__ wpos,
-                          const double* __restrict__ r, double* out, unsigned int* mx) {
+// (w = omega offset of the slot, x, y = transverse positions, rf = r in FP32) and
+// mx = max |S|^2 (bit pattern).  A block takes whole omega-slots (w is the block's constant
+// there) and walks their rows; blockDim.x = Nx clamped to [32, 256] (a multiple of 32).
+__global__ void k_moments(const float2* __restrict__ S, int Nt, int NP, int Nx, int Ny, int SLO,
+                          const float* __restrict__ wpos, const float* __restrict__ rf, double* out, unsigned int* mx) {
     __shared__ double sh[32];
     double m[7] = {0, 0, 0, 0, 0, 0, 0};
     float vmax = 0.0f;
-    const long blk = (long)NP * SLO;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-        const float2 v = S[i];
-        const float e = fmaf(v.x, v.x, v.y * v.y);
-        const long rem = i % blk;
-        const int q = (int)(rem / SLO);
-        const int slot = (int)(i / blk) * SLO + (int)(rem % SLO);
-        const double w = wpos[slot], x = r[q % Nx], y = r[q / Nx];
-        m[0] += e;
-        m[1] += w * e;
-        m[2] += w * w * e;
-        m[3] += x * e;
-        m[4] += x * x * e;
-        m[5] += y * e;
-        m[6] += y * y * e;
-        vmax = fmaxf(vmax, e);
+    for (int slot = blockIdx.x; slot < Nt; slot += gridDim.x) {
+        const size_t base = (size_t)(slot / SLO) * NP * SLO + (slot % SLO);
+        double a[5] = {0, 0, 0, 0, 0};   // e, x e, x^2 e, y e, y^2 e of this slot
+        for (int y0 = 0; y0 < Ny; y0 += kRun) {
+            float p[5] = {0, 0, 0, 0, 0};
+            const int y1 = y0 + kRun < Ny ? y0 + kRun : Ny;
+            for (int y = y0; y < y1; y++) {
+                const float yv = rf[y];
+                for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+                    const float2 v = S[base + (size_t)(y * Nx + x) * SLO];
+                    const float e = fmaf(v.x, v.x, v.y * v.y);
+                    const float xv = rf[x], xe = xv * e, ye = yv * e;
+                    p[0] += e;
+                    p[1] += xe;
+                    p[2] = fmaf(xv, xe, p[2]);
+                    p[3] += ye;
+                    p[4] = fmaf(yv, ye, p[4]);
+                    vmax = fmaxf(vmax, e);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 5; k++) a[k] += (double)p[k];
+        }
+        const double w = wpos[slot];
+        m[0] += a[0];
+        m[1] += w * a[0];
+        m[2] += w * w * a[0];
+        m[3] += a[1];
+        m[4] += a[2];
+        m[5] += a[3];
+        m[6] += a[4];
     }
     for (int k = 0; k < 7; k++) {
         const double t = block_sum(m[k], sh);
@@ -238,9 +277,14 @@ __global__ void k_spec(const float2* __restrict__ S, int NP, int SLO, const int*
     const int pos = blockIdx.x;
     double acc = 0.0;
     const size_t base = (size_t)(pos / SLO) * NP * SLO + (pos % SLO);
-    for (int q = threadIdx.x; q < NP; q += blockDim.x) {
-        const float2 v = S[base + (size_t)q * SLO];
-        acc += (double)fmaf(v.x, v.x, v.y * v.y);
+    int q = threadIdx.x;
+    while (q < NP) {
+        float part = 0.0f;
+        for (int j = 0; j < kRun && q < NP; j++, q += blockDim.x) {
+            const float2 v = S[base + (size_t)q * SLO];
+            part = fmaf(v.x, v.x, fmaf(v.y, v.y, part));
+        }
+        acc += (double)part;
     }
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) spec[ft[pos]] = acc * scale;
@@ -279,6 +323,7 @@ __global__ void k_adk(long n, const double* __restrict__ E, double* r1, double* 
 struct TableSet {
     float4* Rx = nullptr;       // double-float Rx, Nx
     float4* RyD = nullptr;      // double-float Ry x D, Ny * Nt
+    float4* RyDT = nullptr;     // the same, slot-major: Nt * Ny
     double2* f64 = nullptr;     // FP64 Rx (Nx), Ry (Ny), D (Nt); base of the allocation
 };
 
@@ -315,6 +360,7 @@ struct mpc_ctx {
     int *dfx = nullptr, *dfy = nullptr, *dft = nullptr;
     std::vector<int> hfx, hfy, hft;
     double *dwr = nullptr, *dbetas = nullptr, *dr = nullptr;
+    float* rf = nullptr;        // r in FP32 (after dr in the same allocation)
     float2 *lensx = nullptr, *lensy = nullptr;
     double* penergy = nullptr;  // NP
     double* dred = nullptr;     // reduction outputs (2 Nt + Nx + Ny + 64 doubles)
@@ -418,19 +464,20 @@ static void build_nl(mpc_ctx* c) {
 // one allocation: FP64 factors (Nx + Ny + Nt double2), double-float Rx (Nx) and RyD (Ny*Nt)
 static int alloc_tables(mpc_ctx* c, TableSet* t) {
     const size_t n64 = (size_t)(c->Nx + c->Ny + c->Nt);
-    const size_t bytes = n64 * sizeof(double2) + ((size_t)c->Nx + (size_t)c->Ny * c->Nt) * sizeof(float4);
+    const size_t bytes = n64 * sizeof(double2) + ((size_t)c->Nx + 2 * (size_t)c->Ny * c->Nt) * sizeof(float4);
     char* buf = nullptr;
     CK(cudaMalloc(&buf, bytes), "cudaMalloc tables");
     t->f64 = reinterpret_cast<double2*>(buf);
     t->Rx = reinterpret_cast<float4*>(buf + n64 * sizeof(double2));
     t->RyD = t->Rx + c->Nx;
+    t->RyDT = t->RyD + (size_t)c->Ny * c->Nt;
     return MPC_OK;
 }
 
 static int split_tables(mpc_ctx* c, const TableSet& t) {
     const long n = (long)c->Ny * c->Nt;
     k_split<<<(int)((n + 255) / 256), 256, 0, c->st>>>(t.f64, t.f64 + c->Nx, t.f64 + c->Nx + c->Ny, c->Nx, c->Ny,
-                                                       c->Nt, t.Rx, t.RyD);
+                                                       c->Nt, t.Rx, t.RyD, t.RyDT);
     CK(cudaGetLastError(), "k_split");
     c->launches++;
     return MPC_OK;
@@ -489,9 +536,9 @@ static int launch_plane(mpc_ctx* c, const float2* in, float2* out, const TableSe
     a.out = out;
     a.twx = c->twx;
     a.twy = c->twy;
-    a.t1 = PlaneTables{t1.Rx, t1.RyD};
+    a.t1 = PlaneTables{t1.Rx, t1.RyD, t1.RyDT};
     if (t2) {
-        a.t2 = PlaneTables{t2->Rx, t2->RyD};
+        a.t2 = PlaneTables{t2->Rx, t2->RyD, t2->RyDT};
         a.lens = 1;
     } else {
         a.t2 = a.t1;
@@ -644,12 +691,17 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
         TRYC(cudaMalloc(&c->wpos, sizeof(float) * Nt), "cudaMalloc wpos");
         TRYC(cudaMemcpy(c->wpos, wp.data(), sizeof(float) * Nt, cudaMemcpyHostToDevice), "copy wpos");
     }
-    TRYC(cudaMalloc(&c->dwr, sizeof(double) * (Ny + Nt + Ny)), "cudaMalloc FP64 grids");
+    TRYC(cudaMalloc(&c->dwr, sizeof(double) * (Ny + Nt + Ny) + sizeof(float) * Ny), "cudaMalloc FP64 grids");
     c->dbetas = c->dwr + Ny;
     c->dr = c->dbetas + Nt;
+    c->rf = reinterpret_cast<float*>(c->dr + Ny);
     TRYC(cudaMemcpy(c->dwr, c->wr.data(), sizeof(double) * Ny, cudaMemcpyHostToDevice), "copy wr");
     TRYC(cudaMemcpy(c->dbetas, c->betas.data(), sizeof(double) * Nt, cudaMemcpyHostToDevice), "copy betas");
     TRYC(cudaMemcpy(c->dr, c->r.data(), sizeof(double) * Ny, cudaMemcpyHostToDevice), "copy r");
+    {
+        std::vector<float> rf(c->r.begin(), c->r.end());
+        TRYC(cudaMemcpy(c->rf, rf.data(), sizeof(float) * Ny, cudaMemcpyHostToDevice), "copy r (FP32)");
+    }
     TRYC(cudaMalloc(&c->lensx, sizeof(float2) * (Nx + Ny)), "cudaMalloc lens");
     c->lensy = c->lensx + Nx;
     if (p->bounce_mode == MPC_BOUNCE_LENS && p->roc != 0.0) {
@@ -1497,8 +1549,8 @@ int mpc_features(mpc_ctx* c, float* f) {
     int rc = mpc_step_stats(c, stt, 0);
     if (rc) return rc;
     CK(cudaMemsetAsync(c->dmom, 0, 8 * sizeof(double), c->st), "memset moments");
-    k_moments<<<c->nsm * 4, 256, 0, c->st>>>(c->S, c->N, (int)c->NP, c->Nx, c->ops->SLO, c->wpos, c->dr, c->dmom,
-                                            reinterpret_cast<unsigned int*>(c->dmom + 7));
+    k_moments<<<c->Nt, c->Nx < 32 ? 32 : (c->Nx < 256 ? c->Nx : 256), 0, c->st>>>(c->S, c->Nt, (int)c->NP, c->Nx, c->Ny, c->ops->SLO, c->wpos,
+                                                             c->rf, c->dmom, reinterpret_cast<unsigned int*>(c->dmom + 7));
     CK(cudaGetLastError(), "k_moments");
     c->launches++;
     double m[8];
@@ -1537,9 +1589,64 @@ int mpc_features(mpc_ctx* c, float* f) {
     return MPC_OK;
 }
 
-int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, int fallback_len,
-                    mpc_learned_stats* out) {
-    if (!c || !mlp || !out || !(safety > 0) || check_every < 1 || fallback_len < 0)
+// Plain split steps of the learned controller with their adjacent linear half steps merged: the
+// field is left with the last step's second half step pending (zd, zp), which the next step's
+// first plane sweep takes together with its own first half (one sweep instead of two), and which
+// flush_half applies on its own before anything that needs the whole step.
+struct HalfStep {
+    int pending = 0;
+    double zd = 0.0, zp = 0.0;   // diffraction (signed) and dispersion lengths of the pending half
+};
+
+static int flush_half(mpc_ctx* c, HalfStep* h) {
+    if (!h->pending) return MPC_OK;
+    const double sN = 1.0 / ((double)c->NP * c->Nt);
+    TableSet t;
+    int rc;
+    recycle_tables(c);
+    if ((rc = get_tables(c, h->zd, h->zp, sN, &t))) return rc;
+    if ((rc = launch_plane(c, c->S, c->S, t, nullptr))) return rc;
+    h->pending = 0;
+    return MPC_OK;
+}
+
+// one split step of dz at state.z (mpc_step's arithmetic), its second half step left pending;
+// a step that ends on or crosses a mirror plane is completed and bounced (lens, loss)
+static int merged_step(mpc_ctx* c, double dz, HalfStep* h) {
+    mpc_state& st = c->state;
+    int signum = pass_sign(st.z, c->p.Cav);  // calcexpR (propagation.c:377-382)
+    if (-st.signmem == signum) st.signmem = -st.signmem;
+    if (c->p.bounce_mode == MPC_BOUNCE_LENS) signum = 1;
+    const double sNP = 1.0 / (double)c->NP, sN = 1.0 / ((double)c->NP * c->Nt);
+    TableSet t;
+    int rc;
+    recycle_tables(c);
+    if (h->pending) {
+        if ((rc = get_tables(c, h->zd + signum * dz / 2, h->zp + dz / 2, sN, &t))) return rc;
+    } else if ((rc = get_tables(c, signum * dz / 2, dz / 2, sNP, &t))) {
+        return rc;
+    }
+    if ((rc = launch_plane(c, c->S, c->S, t, nullptr))) return rc;
+    if ((rc = pencil_step(c, dz))) return rc;
+    h->pending = 1;
+    h->zd = signum * dz / 2;
+    h->zp = dz / 2;
+    const double z0 = st.z;
+    st.z = z0 + dz;
+    const int nb = bounces_between(z0, st.z, c->p.Cav);
+    if (nb > 0 && (rc = flush_half(c, h))) return rc;
+    for (int b = 0; b < nb; b++) {
+        if (c->p.bounce_mode == MPC_BOUNCE_LENS && (rc = launch_plane(c, c->S, c->S, c->ident, &c->ident))) return rc;
+        st.puls_e *= c->p.Ab_M;
+    }
+    if (st.z > c->p.dist) st.z = c->p.dist;
+    st.nstep++;
+    return MPC_OK;
+}
+
+int mpc_run_learned_hold(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, int fallback_len, int hold,
+                         mpc_learned_stats* out) {
+    if (!c || !mlp || !out || !(safety > 0) || check_every < 1 || fallback_len < 0 || hold < 1)
         return fail(MPC_ERR_ARG, "bad argument");
     if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
     memset(out, 0, sizeof *out);
@@ -1549,10 +1656,13 @@ int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, in
     double err;
     float f[MPC_NFEATURES], stt[4];
     int fb = 1;  // open with one step-doubling attempt (it also provides the first statistics)
-    int since_check = 0;
-    double dz_last = st.dzz;
+    int since_check = 0, held = 0;
+    double dz_last = st.dzz, dz_net = 0.0;
+    HalfStep half;
+    recycle_tables(c);
     while (st.z < dist * (1.0 - 1e-12)) {
         if (fb > 0) {
+            if ((rc = flush_half(c, &half))) return rc;
             const double h = st.dzz;
             if ((rc = mpc_step_double(c, nullptr, nullptr, &bad, &err))) return rc;
             out->fallback_attempts++;
@@ -1561,17 +1671,23 @@ int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, in
                 fb--;
                 dz_last = 2.0 * h;
             }
+            held = 0;
             continue;
         }
-        if ((rc = mpc_features(c, f))) return rc;
-        if ((rc = mpc_step_stats(c, stt, 1))) return rc;
-        float y = 0.0f;
-        if ((rc = mpc_mlp_predict1(mlp, f, &y))) return fail(rc, "network prediction failed");
-        double dz = safety * Cav * exp((double)y);
-        if (!(dz > 0) || !isfinite(dz)) dz = dz_last;
-        dz = fmin(dz, 2.0 * dz_last);
-        dz = Cav * exp2(floor(16.0 * log2(dz / Cav)) / 16.0);   // cached phase tables stay few
-        dz = fmax(dz, dzmin);
+        if (held == 0) {   // a new prediction: features of the whole step
+            if ((rc = flush_half(c, &half))) return rc;
+            if ((rc = mpc_features(c, f))) return rc;
+            if ((rc = mpc_step_stats(c, stt, 1))) return rc;
+            float y = 0.0f;
+            if ((rc = mpc_mlp_predict1(mlp, f, &y))) return fail(rc, "network prediction failed");
+            dz_net = safety * Cav * exp((double)y);
+            if (!(dz_net > 0) || !isfinite(dz_net)) dz_net = dz_last;
+            dz_net = fmin(dz_net, 2.0 * dz_last);
+            dz_net = Cav * exp2(floor(16.0 * log2(dz_net / Cav)) / 16.0);   // cached phase tables stay few
+            dz_net = fmax(dz_net, dzmin);
+            held = hold;
+        }
+        double dz = dz_net;
         // land on the next mirror plane rather than step across it, so each bounce is applied
         // where the mirror is
         const double next_plane = (floor(st.z / Cav + 1e-9) + 1.0) * Cav;
@@ -1580,9 +1696,11 @@ int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, in
         if (++since_check >= check_every) {
             since_check = 0;
             out->checks++;
+            if ((rc = flush_half(c, &half))) return rc;
             st.dzz = dz / 2.0;
             if ((rc = mpc_step_double(c, nullptr, nullptr, &bad, &err))) return rc;
             out->executed_steps += 3;
+            held = 0;
             if (bad || err > c->p.def_err) {
                 out->check_failures++;
                 fb = fallback_len;
@@ -1591,7 +1709,8 @@ int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, in
             }
             continue;
         }
-        if ((rc = mpc_step(c, dz))) return rc;
+        if ((rc = merged_step(c, dz, &half))) return rc;
+        held--;
         out->steps++;
         out->executed_steps++;
         out->dz_min = out->steps == 1 ? dz : fmin(out->dz_min, dz);
@@ -1599,7 +1718,12 @@ int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, in
         dz_last = dz;
         st.dzz = dz;
     }
-    return MPC_OK;
+    return flush_half(c, &half);
+}
+
+int mpc_run_learned(mpc_ctx* c, mpc_mlp* mlp, double safety, int check_every, int fallback_len,
+                    mpc_learned_stats* out) {
+    return mpc_run_learned_hold(c, mlp, safety, check_every, fallback_len, 1, out);
 }
 
 int mpc_mirror_bounce(mpc_ctx* c, int mode) {

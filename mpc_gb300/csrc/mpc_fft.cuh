@@ -358,8 +358,9 @@ __device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, const S
 // of the forward transform, the operator and the span-1 stage of the inverse work on the same R
 // positions of a line, so they run in registers in one pass (op(v, pos0, line) multiplies the
 // values of positions pos0 .. pos0 + R - 1).  Same arithmetic as dif_all, a pass applying op,
-// then dit_all.  Ends with a __syncthreads.
-template <int N, int L, class V, int NTH, int UNR, class OP>
+// then dit_all.  Ends with a __syncthreads unless TAIL = false (the caller then fences and
+// synchronises itself).
+template <int N, int L, class V, int NTH, int UNR, class OP, bool TAIL = true>
 __device__ __forceinline__ void dif_op_dit(float2* s, Twiddles tw, int tid, const OP& op) {
     constexpr int R = Radix<L>::R;
     if constexpr (L / R > 1) {
@@ -367,7 +368,7 @@ __device__ __forceinline__ void dif_op_dit(float2* s, Twiddles tw, int tid, cons
         __syncthreads();
         dif_op_dit<N, L / R, V, NTH, UNR, OP>(s, tw, tid, op);
         dit_stage<N, L, V, NTH, UNR>(s, tw, tid);
-        __syncthreads();
+        if constexpr (TAIL) __syncthreads();
     } else {
         constexpr int TOT = (N / R) * V::NLINES;
 #pragma unroll UNR
@@ -384,7 +385,7 @@ __device__ __forceinline__ void dif_op_dit(float2* s, Twiddles tw, int tid, cons
 #pragma unroll
             for (int q = 0; q < R; q++) p0[V::at(q, 0) - V::at(0, 0)] = v[q];
         }
-        __syncthreads();
+        if constexpr (TAIL) __syncthreads();
     }
 }
 

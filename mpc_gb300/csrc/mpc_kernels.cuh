@@ -779,6 +779,7 @@ __global__ void __launch_bounds__(PencilCfg<NT, P, SLO, CH>::TH, (PencilCfg<NT, 
 struct PlaneTables {
     const float4* Rx;   // Nx, x position order: exp(-i zd kx^2 / (2 k0))
     const float4* RyD;  // Ny * Nt, [y position][slot position]: Ry(ky) D(omega) scale
+    const float4* RyDT; // the same factors slot-major, Nt * Ny: [slot position][y position]
 };
 
 struct PlaneArgs {
@@ -879,6 +880,15 @@ struct YFactors {
         const float4* f = RyD + (size_t)y0 * Nt + slot;
 #pragma unroll
         for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], __ldg(&f[(size_t)q * Nt]));
+    }
+};
+// Rx(px) (double-float) at row-view positions x, from shared or global memory
+struct XFactorsAny {
+    const float4* Rx;
+    template <int R>
+    __device__ __forceinline__ void operator()(float2 (&v)[R], int x0, int) const {
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], Rx[x0 + q]);
     }
 };
 // Rx(px) (double-float) at row-view positions x (FFT position order).
@@ -1021,26 +1031,28 @@ struct StripXView {
 template <int NX, int NY, int CXS>
 struct StripYCfg {
     static constexpr int SIZE = NY * CXS;
-    static constexpr int SMEM = SIZE * 8 + twiddle_bytes(NY);
+    // [strip][the slot's NY factors Ry(y) D(slot), 16 B each][W_NY twiddles]
+    static constexpr int SMEM = SIZE * 8 + NY * 16 + twiddle_bytes(NY);
     // at least 16 columns: the rows of a warp's butterfly loads then fill all 32 banks
     static_assert(CXS >= 16 && CXS % 2 == 0 && NX % CXS == 0, "whole float4 column strips");
 };
 template <int NX, int NY, int RYS>
 struct StripXCfg {
     static constexpr int SIZE = RYS * (NX + 1);
-    static constexpr int SMEM = ((SIZE * 8 + 15) / 16) * 16 + twiddle_bytes(NX);
+    // rows of up to 256 points: the x factors of both tables staged in shared memory once per CTA
+    static constexpr bool XSTAGE = NX <= 256;
+    static constexpr int SMEM = ((SIZE * 8 + 15) / 16) * 16 + (XSTAGE ? 2 * NX * 16 : 0) + twiddle_bytes(NX);
     static_assert(NY % RYS == 0 && NX % 2 == 0, "whole row strips");
 };
 
-// Ry(py) D(slot) at strip positions y of any line (the strip is one omega-plane)
-struct YSlotFactors {
-    const float4* __restrict__ RyD;
-    int Nt, slot;
+
+// Ry(y) D(slot) of the unit's slot from shared memory (staged once per unit)
+struct YSmemFactors {
+    const float4* f;   // NY factors of the unit's slot, shared memory
     template <int R>
     __device__ __forceinline__ void operator()(float2 (&v)[R], int y0, int) const {
-        const float4* f = RyD + (size_t)y0 * Nt + slot;
 #pragma unroll
-        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], __ldg(&f[(size_t)q * Nt]));
+        for (int q = 0; q < R; q++) v[q] = cmul_df(v[q], f[y0 + q]);
     }
 };
 
@@ -1056,25 +1068,28 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_y_ke
     using V = StripYView<NY, CXS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
-    unsigned char* tw_mem = smem_raw + C::SIZE * 8;
+    float4* fac = reinterpret_cast<float4*>(smem_raw + C::SIZE * 8);
+    unsigned char* tw_mem = smem_raw + C::SIZE * 8 + NY * 16;
     const int tid = threadIdx.x;
     stage_twiddles<NY, NTHR>(tw_mem, a.twy, tid);
     const Twiddles tw = Twiddles::packed(tw_mem, NY);
     __syncthreads();
-    const float4* RyD = second ? a.t2.RyD : a.t1.RyD;
+    const float4* RyDT = second ? a.t2.RyDT : a.t1.RyDT;
     constexpr int STRIPS = NX / CXS;
     constexpr int F4_ROW = CXS / 2;
     const int units = a.Nt * STRIPS;
     for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
         const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
         const float4* g4 = reinterpret_cast<const float4*>(a.in) + ((size_t)slot * a.NP + x0) / 2;
+        // the slot's factors, shared by the strip's CXS columns
+        for (int y = tid; y < NY; y += NTHR) fac[y] = __ldg(&RyDT[(size_t)slot * NY + y]);
 #pragma unroll 8
         for (int f = tid; f < NY * F4_ROW; f += NTHR) {
             const int y = f / F4_ROW, c = f - y * F4_ROW;
             reinterpret_cast<float4*>(s)[(y * CXS) / 2 + c] = __ldg(&g4[(size_t)y * (NX / 2) + c]);
         }
         __syncthreads();
-        dif_op_dit<NY, NY, V, NTHR, 1>(s, tw, tid, YSlotFactors{RyD, a.Nt, slot});
+        dif_op_dit<NY, NY, V, NTHR, 1>(s, tw, tid, YSmemFactors{fac});
         float4* o4 = reinterpret_cast<float4*>(a.out) + ((size_t)slot * a.NP + x0) / 2;
 #pragma unroll 8
         for (int f = tid; f < NY * F4_ROW; f += NTHR) {
@@ -1087,15 +1102,19 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_y_ke
 
 // y part with TMA staging: a persistent CTA walks its units (slot, strip of CXS columns) with
 // NBUF unit buffers in shared memory; one thread keeps NBUF - 1 units in flight as 2-D bulk tensor
-// loads (box: CXS complex columns x NY rows of one omega-plane, landing in the StripYView layout),
-// and each finished unit leaves by a bulk tensor store, so no thread spends instructions or
-// registers on moving the strips.  tin / tout map the field as float rows of 2 Nx values, Ny * Nt
-// rows.  A load that does not arrive within the wait limit sets *err and ends the kernel.
+// loads (box: CXS complex columns x NY rows of one omega-plane, landing in the StripYView layout)
+// plus a bulk copy of the slot's NY factors Ry(y) D(slot) (the slot-major table, 16 B each) on
+// the same mbarrier, and each finished unit leaves by a bulk tensor store, so no thread spends
+// instructions or registers on moving the strips and every factor is read from shared memory
+// (all CXS columns of a row share it).  tin / tout map the field as float rows of 2 Nx values,
+// Ny * Nt rows.  A load that does not arrive within the wait limit sets *err and ends the kernel.
 template <int NX, int NY, int CXS>
 struct StripYTmaCfg {
     static constexpr int UNIT_BYTES = NY * CXS * 8;
+    static constexpr int FAC_BYTES = NY * 16;   // one slot's Ry(y) D(slot) factors, double-float
     static_assert(UNIT_BYTES % 128 == 0 && CXS * 8 % 16 == 0, "unit buffers of whole 128 B lines");
-    static constexpr __host__ __device__ int TW_OFF(int nbuf) { return nbuf * UNIT_BYTES; }
+    static constexpr __host__ __device__ int FAC_OFF(int nbuf) { return nbuf * UNIT_BYTES; }
+    static constexpr __host__ __device__ int TW_OFF(int nbuf) { return FAC_OFF(nbuf) + nbuf * FAC_BYTES; }
     static constexpr __host__ __device__ int BAR_OFF(int nbuf) { return TW_OFF(nbuf) + ((twiddle_bytes(NY) + 15) / 16) * 16; }
     static constexpr __host__ __device__ int SMEM(int nbuf) { return 128 + BAR_OFF(nbuf) + nbuf * 8 + 16; }
 };
@@ -1122,14 +1141,18 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
     }
     stage_twiddles<NY, NTHR>(tw_mem, a.twy, tid);
     const Twiddles tw = Twiddles::packed(tw_mem, NY);
-    const float4* RyD = second ? a.t2.RyD : a.t1.RyD;
+    const float4* RyDT = second ? a.t2.RyDT : a.t1.RyDT;
     __syncthreads();
     auto buf = [&](int k) { return reinterpret_cast<float2*>(smem_raw + (k % NBUF) * C::UNIT_BYTES); };
-    auto issue = [&](int k) {   // load my k-th unit
+    auto fac = [&](int k) {
+        return reinterpret_cast<float4*>(smem_raw + C::FAC_OFF(NBUF) + (k % NBUF) * C::FAC_BYTES);
+    };
+    auto issue = [&](int k) {   // load my k-th unit and its slot's factors
         const int unit = (int)blockIdx.x + k * (int)gridDim.x;
         const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
-        mbar_arrive_expect_tx(&bars[k % NBUF], C::UNIT_BYTES);
+        mbar_arrive_expect_tx(&bars[k % NBUF], C::UNIT_BYTES + C::FAC_BYTES);
         tma_load_2d(buf(k), &tin, 2 * x0, slot * NY, &bars[k % NBUF]);
+        bulk_load(fac(k), RyDT + (size_t)slot * NY, C::FAC_BYTES, &bars[k % NBUF]);
     };
     if (tid == 0)
         for (int k = 0; k < NBUF - 1 && k < nmine; k++) issue(k);
@@ -1151,8 +1174,8 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         }
         mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1));   // completed: returns at once
         float2* s = buf(k);
-        dif_op_dit<NY, NY, V, NTHR, 1>(s, tw, tid, YSlotFactors{RyD, a.Nt, slot});
-        fence_proxy_async_smem();
+        dif_op_dit<NY, NY, V, NTHR, 1, YSmemFactors, false>(s, tw, tid, YSmemFactors{fac(k)});
+        fence_proxy_async_smem();   // this thread's results, before the bulk store reads them
         __syncthreads();
         if (tid == 0) {
             tma_store_2d(&tout, 2 * x0, slot * NY, s);
@@ -1206,7 +1229,7 @@ __device__ __forceinline__ void x16_span16(unsigned char* buf, Twiddles tw, int 
 }
 
 template <int NTHR>
-__device__ __forceinline__ void x16_middle(unsigned char* buf, const float4* __restrict__ Rx, int tid) {
+__device__ __forceinline__ void x16_middle(unsigned char* buf, const float4* Rx, int tid) {
     // the span-1 forward stage, the Rx factors and the span-1 inverse stage, on 16 consecutive
     // x of one row; rows fastest (8 rows per quarter-warp), pairs of complex per 16-byte access
     for (int item = tid; item < 256; item += NTHR) {
@@ -1221,7 +1244,7 @@ __device__ __forceinline__ void x16_middle(unsigned char* buf, const float4* __r
         }
         dft<16, false>(v);
 #pragma unroll
-        for (int q = 0; q < 16; q++) v[q] = cmul_df(v[q], __ldg(&Rx[16 * b + q]));
+        for (int q = 0; q < 16; q++) v[q] = cmul_df(v[q], Rx[16 * b + q]);   // shared memory
         dft<16, true>(v);
 #pragma unroll
         for (int c = 0; c < 8; c++)
@@ -1230,15 +1253,15 @@ __device__ __forceinline__ void x16_middle(unsigned char* buf, const float4* __r
     }
 }
 
-// IFFT_x Rx FFT_x on the 16 rows of a swizzled unit; ends with a CTA barrier
-template <int NTHR>
+// IFFT_x Rx FFT_x on the 16 rows of a swizzled unit; ends with a CTA barrier unless TAIL = false
+template <int NTHR, bool TAIL = true>
 __device__ __forceinline__ void x16_linear(unsigned char* buf, Twiddles tw, const float4* Rx, int tid) {
     x16_span16<NTHR>(buf, tw, tid, false);
     __syncthreads();
     x16_middle<NTHR>(buf, Rx, tid);
     __syncthreads();
     x16_span16<NTHR>(buf, tw, tid, true);
-    __syncthreads();
+    if constexpr (TAIL) __syncthreads();
 }
 
 template <int NY, int NTHR, int NBUF>
@@ -1250,11 +1273,17 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
     // unit buffers on a 1024-byte boundary of the shared window, where the 128-byte swizzle's
     // pattern starts (the launch adds 1 KB of slack)
     unsigned char* smem_raw = smem_dyn + ((1024u - (smem_addr(smem_dyn) & 1023u)) & 1023u);
-    unsigned char* tw_mem = smem_raw + NBUF * UNIT_BYTES;
+    float4* rx1 = reinterpret_cast<float4*>(smem_raw + NBUF * UNIT_BYTES);   // Rx of t1, then of t2
+    float4* rx2 = rx1 + NX;
+    unsigned char* tw_mem = reinterpret_cast<unsigned char*>(rx2 + NX);
     uint64_t* bars = reinterpret_cast<uint64_t*>(tw_mem + ((twiddle_bytes(NX) + 15) / 16) * 16);
     int& s_arrived = *reinterpret_cast<int*>(bars + NBUF);
     const int tid = threadIdx.x;
     constexpr int STRIPS = NY / RYS;
+    for (int i = tid; i < NX; i += NTHR) {   // the x factors of both tables, once per CTA
+        rx1[i] = __ldg(&a.t1.Rx[i]);
+        rx2[i] = __ldg(&a.t2.Rx[i]);
+    }
     const int units = a.Nt * STRIPS;
     const int nmine = blockIdx.x < units ? (units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tid == 0) {
@@ -1295,17 +1324,19 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         }
         mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1));   // completed: returns at once
         unsigned char* u = buf(k);
-        x16_linear<NTHR>(u, tw, a.t1.Rx, tid);
         if (a.lens) {
+            x16_linear<NTHR>(u, tw, rx1, tid);
             for (int e = tid; e < RYS * NX; e += NTHR) {
                 const int x = e % NX, r = e / NX;
                 float2* pe = reinterpret_cast<float2*>(u + xsw_offset(x, r));
                 *pe = cmul(*pe, cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y0 + r])));
             }
             __syncthreads();
-            x16_linear<NTHR>(u, tw, a.t2.Rx, tid);
+            x16_linear<NTHR, false>(u, tw, rx2, tid);
+        } else {
+            x16_linear<NTHR, false>(u, tw, rx1, tid);
         }
-        fence_proxy_async_smem();
+        fence_proxy_async_smem();   // this thread's results, before the bulk stores read them
         __syncthreads();
         if (tid == 0) {
 #pragma unroll 1
@@ -1327,10 +1358,21 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_x_ke
     using V = StripXView<NX, RYS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
-    unsigned char* tw_mem = smem_raw + ((C::SIZE * 8 + 15) / 16) * 16;
+    float4* rx_s = reinterpret_cast<float4*>(smem_raw + ((C::SIZE * 8 + 15) / 16) * 16);
+    unsigned char* tw_mem = reinterpret_cast<unsigned char*>(rx_s) + (C::XSTAGE ? 2 * NX * 16 : 0);
     const int tid = threadIdx.x;
     stage_twiddles<NX, NTHR>(tw_mem, a.twx, tid);
     const Twiddles tw = Twiddles::packed(tw_mem, NX);
+    const float4* rx1 = a.t1.Rx;
+    const float4* rx2 = a.t2.Rx;
+    if constexpr (C::XSTAGE) {
+        for (int i = tid; i < NX; i += NTHR) {
+            rx_s[i] = __ldg(&a.t1.Rx[i]);
+            rx_s[NX + i] = __ldg(&a.t2.Rx[i]);
+        }
+        rx1 = rx_s;
+        rx2 = rx_s + NX;
+    }
     __syncthreads();
     constexpr int STRIPS = NY / RYS;
     constexpr int F4_ROW = NX / 2;
@@ -1346,7 +1388,7 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_x_ke
             s[V::at(2 * c + 1, r)] = make_float2(v.z, v.w);
         }
         __syncthreads();
-        dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactors{a.t1.Rx});
+        dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactorsAny{rx1});
         if (a.lens) {
             for (int e = tid; e < RYS * NX; e += NTHR) {
                 const int x = e % NX, r = e / NX;
@@ -1354,7 +1396,7 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_x_ke
                 s[idx] = cmul(s[idx], cmul(__ldg(&a.lensx[x]), __ldg(&a.lensy[y0 + r])));
             }
             __syncthreads();
-            dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactors{a.t2.Rx});
+            dif_op_dit<NX, NX, V, NTHR, 1>(s, tw, tid, XFactorsAny{rx2});
         }
         float4* o4 = reinterpret_cast<float4*>(a.out) + ((size_t)slot * a.NP + (size_t)y0 * NX) / 2;
 #pragma unroll 8

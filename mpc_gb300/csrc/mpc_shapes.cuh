@@ -92,7 +92,7 @@ struct Shape {
     static constexpr int TCX = 16, TTH = 256, TNB = 3;
     static_assert(PL < 3 || (NX % TCX == 0 && NY <= 256), "TMA boxes: 16 columns, at most 256 rows");
     static_assert(PL != 4 || (NX == 256 && NY % 16 == 0), "TMA x part: rows of 256, strips of 16 rows");
-    static constexpr int XSMEM = 1024 + 3 * 32768 + ((twiddle_bytes(256) + 15) / 16) * 16 + 3 * 8 + 16;
+    static constexpr int XSMEM = 1024 + 3 * 32768 + 2 * 256 * 16 + ((twiddle_bytes(256) + 15) / 16) * 16 + 3 * 8 + 16;
     static_assert(SLO == 1 || SLO == 2, "slot interleave");
     static_assert(PT == 128 || PT == 256 || PT == 512, "plane threads");
     static_assert(P >= 4 && P <= NX * NY, "pencil tile must fit the grid");

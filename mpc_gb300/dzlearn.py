@@ -137,9 +137,11 @@ def run_plain(cfg, variant: int = -1, def_err: float | None = None, land: bool =
         return prop.download(), 3 * attempts, dt
 
 
-def run_learned(cfg, mlp, safety: float = 0.9, check_every: int = 8, fallback_len: int = 4, variant: int = -1):
+def run_learned(cfg, mlp, safety: float = 0.9, check_every: int = 8, fallback_len: int = 4, variant: int = -1,
+                hold: int = 1):
     """The learned controller to dist: (field, statistics, seconds).  Its own steps land on the
-    mirror planes, and so do its step-doubling checks and fallbacks."""
+    mirror planes, and so do its step-doubling checks and fallbacks; one prediction serves `hold`
+    consecutive steps."""
     from .capi import Propagator
     p, A = _cell(cfg)
     p = p.copy(land_mirrors=1)
@@ -147,7 +149,7 @@ def run_learned(cfg, mlp, safety: float = 0.9, check_every: int = 8, fallback_le
         prop.upload(A, calibrate=True)
         prop.sync()
         t = time.perf_counter()
-        st = prop.run_learned(mlp, safety=safety, check_every=check_every, fallback_len=fallback_len)
+        st = prop.run_learned(mlp, safety=safety, check_every=check_every, fallback_len=fallback_len, hold=hold)
         prop.sync()
         dt = time.perf_counter() - t
         return prop.download(), st, dt
@@ -168,11 +170,12 @@ def run_reference(cfg, steps_per_pass: int, variant: int = -1):
         return prop.download(), n
 
 
-def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, safeties=(0.9,), **kw) -> list[dict]:
+def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, safeties=(0.9,), plain_tols=(), **kw) -> list[dict]:
     """Per cell: end-field relative L2 error against a fine fixed-step run, executed steps and
     wall time of plain step doubling (as the reference: bounces after the attempt that crosses a
-    mirror plane; and landing on the planes) and of the learned controller at each safety
-    factor.  The err_learned / steps_learned / seconds_learned keys are the first safety's."""
+    mirror plane; and landing on the planes, at the cell's tolerance and at each of plain_tols)
+    and of the learned controller at each safety factor.  The err_learned / steps_learned /
+    seconds_learned keys are the first safety's."""
     rows = []
     for cfg in cfgs:
         cfg = _cell(cfg)
@@ -182,7 +185,10 @@ def evaluate(cfgs: list, mlp, ref_steps_per_pass: int = 2000, safeties=(0.9,), *
         landed, n_landed, t_landed = run_plain(cfg, land=True)
         row = dict(err_plain=float(np.linalg.norm(plain - ref) / nr), steps_plain=int(n_plain), seconds_plain=t_plain,
                    err_plain_landing=float(np.linalg.norm(landed - ref) / nr), steps_plain_landing=int(n_landed),
-                   seconds_plain_landing=t_landed, ref_steps=int(n_ref), learned={})
+                   seconds_plain_landing=t_landed, ref_steps=int(n_ref), learned={}, plain_landing_tol={})
+        for tol in plain_tols:
+            f_t, n_t, t_t = run_plain(cfg, def_err=tol, land=True)
+            row["plain_landing_tol"][tol] = dict(err=float(np.linalg.norm(f_t - ref) / nr), steps=int(n_t), seconds=t_t)
         for sf in safeties:
             learned, st, t_learned = run_learned(cfg, mlp, safety=sf, **kw)
             row["learned"][sf] = dict(err=float(np.linalg.norm(learned - ref) / nr), steps=int(st["executed_steps"]),
@@ -219,6 +225,8 @@ def main(argv=None) -> int:
     e.add_argument("--passes", type=int, default=8)
     e.add_argument("--safety", default="0.9", help="comma-separated safety factors of the learned controller")
     e.add_argument("--ref-steps", type=int, default=2000, help="fixed steps per pass of the reference run")
+    e.add_argument("--plain-tol", default="", help="comma-separated extra tolerances of plain step doubling (landing)")
+    e.add_argument("--hold", type=int, default=1, help="consecutive steps per network prediction")
     a = ap.parse_args(argv)
     if a.cmd == "collect":
         grid = tuple(int(v) for v in a.grid.split(","))
@@ -244,15 +252,20 @@ def main(argv=None) -> int:
         grid = tuple(int(v) for v in a.grid.split(","))
         cfgs = controller_cells(a.seed, a.cells, grid, passes=a.passes, steps_per_pass=400)
         safeties = tuple(float(v) for v in a.safety.split(","))
-        rows = evaluate(cfgs, load(a.model), ref_steps_per_pass=a.ref_steps, safeties=safeties)
+        plain_tols = tuple(float(v) for v in a.plain_tol.split(",") if v)
+        rows = evaluate(cfgs, load(a.model), ref_steps_per_pass=a.ref_steps, safeties=safeties, plain_tols=plain_tols,
+                        hold=a.hold)
         summary = dict(cells=len(rows), grid=grid, passes=a.passes,
                        plain=dict(max_err=max(r["err_plain"] for r in rows), seconds=sum(r["seconds_plain"] for r in rows)),
                        plain_landing=dict(max_err=max(r["err_plain_landing"] for r in rows),
                                           seconds=sum(r["seconds_plain_landing"] for r in rows)),
                        learned={str(sf): dict(max_err=max(r["learned"][sf]["err"] for r in rows),
                                               seconds=sum(r["learned"][sf]["seconds"] for r in rows))
-                                for sf in safeties})
-        print(json.dumps(dict(summary=summary, rows=[{k: (v if k != "learned" else {str(a): b for a, b in v.items()})
+                                for sf in safeties},
+                       plain_landing_tol={str(t): dict(max_err=max(r["plain_landing_tol"][t]["err"] for r in rows),
+                                                       seconds=sum(r["plain_landing_tol"][t]["seconds"] for r in rows))
+                                          for t in plain_tols})
+        print(json.dumps(dict(summary=summary, rows=[{k: ({str(a): b for a, b in v.items()} if isinstance(v, dict) else v)
                                                       for k, v in r.items()} for r in rows])))
     return 0
 

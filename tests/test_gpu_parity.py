@@ -384,6 +384,42 @@ def test_error_paths_return_status_and_leave_the_context_usable(gpu_lib):
     assert set(ERRORS.values()) >= {"MPC_ERR_ARG", "MPC_ERR_SHAPE", "MPC_ERR_STATE"}
 
 
+def test_features_match_numpy_moments(gpu_lib):
+    """The step-size features' moments pass (FP32 runs, FP64 across) against numpy moments of
+    the downloaded field: pulse energy, spectral width and centroid (Parseval over t), beam
+    widths in x and y (the grid positions r)."""
+    from mpc_gb300.capi import Propagator
+    p, A, o = small_cell(Nx=64, Ny=64, Nt=512, window_t=4e-12)
+    with Propagator(p) as prop:
+        prop.upload(A)
+        prop.run_fixed(3)
+        f = prop.features()
+        got = prop.download()
+    HBAR = 1.054560652926899e-34
+    Nt, Ny, Nx = p.Nt, p.Ny, p.Nx
+    F = np.fft.fft(got.reshape(Nt, Ny, Nx), axis=0)
+    P = (np.abs(F) ** 2).sum(axis=(1, 2))
+    w = np.asarray(p.w)[(np.arange(Nt) + Nt // 2) % Nt]
+    E = P.sum()
+    wm = (w * P).sum() / E
+    ws = np.sqrt((w * w * P).sum() / E - wm ** 2)
+    I = (np.abs(got.reshape(Nt, Ny, Nx)) ** 2).sum(axis=0)
+    r = np.asarray(p.r)
+    Ex = I.sum(axis=0)
+    Ey = I.sum(axis=1)
+    xm = (r[:Nx] * Ex).sum() / Ex.sum()
+    xs = np.sqrt((r[:Nx] ** 2 * Ex).sum() / Ex.sum() - xm ** 2)
+    ym = (r[:Ny] * Ey).sum() / Ey.sum()
+    ys = np.sqrt((r[:Ny] ** 2 * Ey).sum() / Ey.sum() - ym ** 2)
+    energy = np.sum(np.abs(got) ** 2) * p.dr ** 2 * p.deltat * HBAR * p.w0
+    window = Nx * p.dr
+    assert f[4] == pytest.approx(np.log10(energy), abs=1e-5)
+    assert f[5] == pytest.approx(ws / p.w0 * 1e2, rel=1e-4)
+    assert f[6] == pytest.approx(wm / p.w0 * 1e2, abs=1e-4 * ws / p.w0 * 1e2)
+    assert f[7] == pytest.approx(xs / window, rel=1e-4)
+    assert f[8] == pytest.approx(ys / window, rel=1e-4)
+
+
 def test_bounded_wait_runs_out_and_reports_timeout(gpu_lib):
     """The device-side waits are bounded: a probe kernel waits on an mbarrier that nothing
     completes, gives up after about a second and leaves its code in the context's error word;
