@@ -136,7 +136,7 @@ WORKLOADS = {
                     desc="multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
                     step="one pass of the cell = 400 split steps",
                     profile={"pencil": ["pencil_step_256x256x2048.txt"],
-                             "plane": ["plane_y_256x256x2048.txt", "plane_x_256x256x2048.txt"]}),
+                             "plane": ["plane_y_tma_256x256x2048.txt", "plane_x_tma_256x256x2048.txt"]}),
     "cell64": dict(config="config1", adaptive=False, per_step=200, cpu_steps=100,
                    desc="multipass cell 64x64x512, fixed split steps, lens mirror, SST + ADK + plasma on",
                    step="one pass of the cell = 200 split steps", profile=None),

@@ -88,7 +88,8 @@ def test_ioniz_every_gas(gpu_lib, gas):
     with Propagator(p) as prop:
         t_g, f_g = prop.ioniz(A)
     print(f"ioniz {gas}: tau_c rel L2 {rel(t_g, tau):.3e}, fe_sp rel L2 {rel(f_g, fe):.3e}")
-    assert rel(t_g, tau) < 1e-5 and fe.max() > 0 and rel(f_g, fe) < 1e-4
+    # measured on GB300: tau_c <= 8e-8, fe_sp <= 1.9e-7 (FP32 within 32-sample chunks, FP64 carries)
+    assert rel(t_g, tau) < 1e-6 and fe.max() > 0 and rel(f_g, fe) < 1e-6
 
 
 def test_ioniz(gpu_lib):
@@ -98,10 +99,10 @@ def test_ioniz(gpu_lib):
     with Propagator(p) as prop:
         tau, fe = prop.ioniz(A)
     print(f"ioniz argon 3 bar: tau_c rel L2 {rel(tau, tau_ref):.3e}, fe_sp rel L2 {rel(fe, fe_ref):.3e}, "
-          f"max ionization fraction {fe_ref.max():.3e}")
-    assert rel(tau, tau_ref) < 1e-5
+          f"max fe_sp {fe_ref.max():.3e}")
+    assert rel(tau, tau_ref) < 1e-6
     assert fe_ref.max() > 0
-    assert rel(fe, fe_ref) < 1e-4
+    assert rel(fe, fe_ref) < 1e-6
 
 
 @pytest.mark.parametrize("plasm,sst", [(1, 1), (0, 1), (1, 0), (0, 0)])
