@@ -313,7 +313,7 @@ def run_gb300(args):
     dom_ms = sweeps[dom][0] / max(1, sweeps[dom][1])
     # one complex64 read + write of the whole field per kernel; the plane sweep of the two-pass
     # variants is two kernels (column strips, then row strips)
-    passes = vinfo.get("PL", 1) if dom == "plane" else 1
+    passes = (2 if vinfo.get("PL", 1) >= 2 else 1) if dom == "plane" else 1
     bytes_launch = 16.0 * p.N * passes
     achieved = bytes_launch / (dom_ms / 1e3) / 1e9
     traffic = profile_traffic(wl["profile"][dom]) if wl["profile"] else None
@@ -330,9 +330,20 @@ def run_gb300(args):
         one_pass()
         prop.download(pin.array)
     e2e_s = time.perf_counter() - t0
+    # where the end-to-end time goes: one more step with the stream drained after each phase
+    t1 = time.perf_counter()
+    prop.upload(pin.array)
+    prop.sync()
+    t2 = time.perf_counter()
+    one_pass()
+    prop.sync()
+    t3 = time.perf_counter()
+    prop.download(pin.array)
+    t4 = time.perf_counter()
+    phase = {"upload_ms": (t2 - t1) * 1e3, "steps_ms": (t3 - t2) * 1e3, "download_ms": (t4 - t3) * 1e3}
     e2e_split = (3 if wl["adaptive"] else 1) * wl["per_step"] * e2e_steps
     e2e = {"value": p.N * e2e_split * world / e2e_s, "unit": "grid-point-steps/s",
-           "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N}
+           "h2d_bytes_per_step": 16 * p.N, "d2h_bytes_per_step": 16 * p.N, "phases_one_step": phase}
 
     # the reference-signature drop-in: mpc_ssfmprop on a host field (pinned), one split step per
     # call with the complex128 field copied in and out every call, as MPC.c's loop would call it

@@ -1147,14 +1147,18 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
     auto fac = [&](int k) {
         return reinterpret_cast<float4*>(smem_raw + C::FAC_OFF(NBUF) + (k % NBUF) * C::FAC_BYTES);
     };
-    auto issue = [&](int k) {   // load my k-th unit and its slot's factors
+    const int warp = tid >> 5, lane = tid & 31;
+    // the copies of a unit are issued by warp 0: lane 0 arms the mbarrier with the unit's bytes and
+    // loads the strip, lane 1 the slot's factors
+    auto issue = [&](int k) {
         const int unit = (int)blockIdx.x + k * (int)gridDim.x;
         const int slot = unit / STRIPS, x0 = (unit - slot * STRIPS) * CXS;
-        mbar_arrive_expect_tx(&bars[k % NBUF], C::UNIT_BYTES + C::FAC_BYTES);
-        tma_load_2d(buf(k), &tin, 2 * x0, slot * NY, &bars[k % NBUF]);
-        bulk_load(fac(k), RyDT + (size_t)slot * NY, C::FAC_BYTES, &bars[k % NBUF]);
+        if (lane == 0) mbar_arrive_expect_tx(&bars[k % NBUF], C::UNIT_BYTES + C::FAC_BYTES);
+        __syncwarp();
+        if (lane == 0) tma_load_2d(buf(k), &tin, 2 * x0, slot * NY, &bars[k % NBUF]);
+        if (lane == 1) bulk_load(fac(k), RyDT + (size_t)slot * NY, C::FAC_BYTES, &bars[k % NBUF]);
     };
-    if (tid == 0)
+    if (warp == 0)
         for (int k = 0; k < NBUF - 1 && k < nmine; k++) issue(k);
     for (int k = 0; k < nmine; k++) {
         const int unit = (int)blockIdx.x + k * (int)gridDim.x;
@@ -1177,11 +1181,13 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         dif_op_dit<NY, NY, V, NTHR, 1, YSmemFactors, false>(s, tw, tid, YSmemFactors{fac(k)});
         fence_proxy_async_smem();   // this thread's results, before the bulk store reads them
         __syncthreads();
-        if (tid == 0) {
-            tma_store_2d(&tout, 2 * x0, slot * NY, s);
-            bulk_commit();
+        if (warp == 0) {
+            if (lane == 0) {
+                tma_store_2d(&tout, 2 * x0, slot * NY, s);
+                bulk_commit();
+            }
             if (k + NBUF - 1 < nmine) {
-                bulk_wait_read<1>();   // the previous unit's store has left its buffer
+                if (lane == 0) bulk_wait_read<1>();   // the previous unit's store has left its buffer
                 issue(k + NBUF - 1);
             }
         }
@@ -1300,14 +1306,17 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         *row0 = slot * NY + y0;
         return y0;
     };
-    auto issue = [&](int k) {   // load my k-th unit: 16 boxes
+    const int warp = tid >> 5, lane = tid & 31;
+    // the copies of a unit are issued by warp 0, one box per lane (lanes 0..15): lane 0 arms the
+    // mbarrier with the unit's bytes first
+    auto issue = [&](int k) {
         int row0;
         coords(k, &row0);
-        mbar_arrive_expect_tx(&bars[k % NBUF], UNIT_BYTES);
-#pragma unroll 1
-        for (int b = 0; b < NX / 16; b++) tma_load_2d(buf(k) + b * 2048, &tin, 32 * b, row0, &bars[k % NBUF]);
+        if (lane == 0) mbar_arrive_expect_tx(&bars[k % NBUF], UNIT_BYTES);
+        __syncwarp();
+        if (lane < NX / 16) tma_load_2d(buf(k) + lane * 2048, &tin, 32 * lane, row0, &bars[k % NBUF]);
     };
-    if (tid == 0)
+    if (warp == 0)
         for (int k = 0; k < NBUF - 1 && k < nmine; k++) issue(k);
     for (int k = 0; k < nmine; k++) {
         int row0;
@@ -1315,10 +1324,14 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         if (tid == 0) s_arrived = mbar_wait(&bars[k % NBUF], (uint32_t)((k / NBUF) & 1)) ? 1 : 0;
         __syncthreads();
         if (!s_arrived) {
-            if (tid == 0) {
-                atomicExch(err, KERR_TMA_TIMEOUT);
-                for (int j = k + 1; j < k + NBUF - 1 && j < nmine; j++) mbar_wait(&bars[j % NBUF], (uint32_t)((j / NBUF) & 1));
-                bulk_wait<0>();
+            if (warp == 0) {
+                if (lane == 0) {
+                    atomicExch(err, KERR_TMA_TIMEOUT);
+                    for (int j = k + 1; j < k + NBUF - 1 && j < nmine; j++)
+                        mbar_wait(&bars[j % NBUF], (uint32_t)((j / NBUF) & 1));
+                }
+                if (lane < NX / 16) bulk_wait<0>();   // each lane's own stores
+                __syncwarp();
             }
             return;
         }
@@ -1338,17 +1351,19 @@ __global__ void __launch_bounds__(NTHR, 512 / NTHR)
         }
         fence_proxy_async_smem();   // this thread's results, before the bulk stores read them
         __syncthreads();
-        if (tid == 0) {
-#pragma unroll 1
-            for (int b = 0; b < NX / 16; b++) tma_store_2d(&tout, 32 * b, row0, u + b * 2048);
-            bulk_commit();
+        if (warp == 0) {
+            if (lane < NX / 16) {
+                tma_store_2d(&tout, 32 * lane, row0, u + lane * 2048);
+                bulk_commit();
+            }
             if (k + NBUF - 1 < nmine) {
-                bulk_wait_read<1>();   // the previous unit's stores have left its buffer
+                // lane b refills box b of the buffer its own store of the previous unit read
+                if (lane < NX / 16) bulk_wait_read<1>();
                 issue(k + NBUF - 1);
             }
         }
     }
-    if (tid == 0) bulk_wait<0>();
+    if (warp == 0 && lane < NX / 16) bulk_wait<0>();
 }
 
 // x part: units are (slot, strip of RYS rows); with the mirror lens, x(t1), the lens, x(t2).
