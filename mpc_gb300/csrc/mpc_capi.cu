@@ -569,6 +569,43 @@ static int ensure_io(mpc_ctx* c, int which) {
     return MPC_OK;
 }
 
+// Field-sized host <-> device copies.  When the host buffer is page-locked and mapped into the
+// device's address space (cudaMallocHost, mpc_host_alloc, cudaHostRegister), SMs move it with
+// 16-byte loads and stores over the host link: on GB300 that runs at the link's rate every time,
+// while a copy-engine transfer that follows a second or more without host-link traffic (the
+// normal case after a propagation pass) was measured at a third of it or less.  Pageable or
+// unaligned buffers go through cudaMemcpyAsync.
+__global__ void k_host_copy(const float4* __restrict__ src, float4* __restrict__ dst, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// the device address of mapped page-locked host memory at p, or null
+static void* mapped_host(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+static int field_copy(mpc_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, const char* what) {
+    const void* host = kind == cudaMemcpyHostToDevice ? src : dst;
+    void* hdev = mapped_host(host);
+    const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0) && bytes % 16 == 0;
+    if (hdev && aligned && bytes > 0) {
+        const float4* s = reinterpret_cast<const float4*>(kind == cudaMemcpyHostToDevice ? hdev : src);
+        float4* d = reinterpret_cast<float4*>(kind == cudaMemcpyHostToDevice ? dst : hdev);
+        k_host_copy<<<2 * c->nsm, 256, 0, c->st>>>(s, d, bytes / 16);
+        CK(cudaGetLastError(), what);
+        c->launches++;
+        return MPC_OK;
+    }
+    CK(cudaMemcpyAsync(dst, src, bytes, kind, c->st), what);
+    return MPC_OK;
+}
+
 extern "C" {
 
 const char* mpc_version(void) { return "mpc_gb300 0.1 (sm_103a)"; }
@@ -895,7 +932,7 @@ int mpc_field_upload(mpc_ctx* c, const double* A, int calibrate) {
     if (!c || !A) return fail(MPC_ERR_ARG, "null argument");
     int rc = ensure_io(c, 0);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    if ((rc = field_copy(c, c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D field"))) return rc;
     double k = 1.0;
     if (calibrate) {
         if (!(c->p.Esig > 0)) return fail(MPC_ERR_ARG, "Esig must be positive to calibrate");
@@ -928,7 +965,7 @@ int mpc_field_download(mpc_ctx* c, double* A) {
     if (!c->have_field) return fail(MPC_ERR_STATE, "no field on the device");
     int rc = exit_to_io(c, 0);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H field");
+    if ((rc = field_copy(c, A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, "D2H field"))) return rc;
     CK(cudaStreamSynchronize(c->st), "download");
     return kernel_errors(c);
 }
@@ -1002,7 +1039,7 @@ int mpc_ssfmprop(mpc_ctx* c, double* A, int sst_on, double dzz, int* signmem, do
     if (change == 1 && (!BP1 || !BP2 || !y1 || !y2 || !bps1 || !bps2)) return fail(MPC_ERR_ARG, "null diagnostic output");
     int rc = ensure_io(c, 0);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    if ((rc = field_copy(c, c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D field"))) return rc;
     PencilArgs a{};
     a.in = c->io;
     a.out = c->S;
@@ -1028,7 +1065,7 @@ int mpc_ssfmprop(mpc_ctx* c, double* A, int sst_on, double dzz, int* signmem, do
     if ((rc = launch_plane(c, c->S, c->S, t2, nullptr))) return rc;
     c->have_field = 1;
     if ((rc = exit_to_io(c, change == 1))) return rc;
-    CK(cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H field");
+    if ((rc = field_copy(c, A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, "D2H field"))) return rc;
     if (change == 1) {
         // propagation.c:334-341, as written (after calcexpR the condition cannot hold)
         const int s2 = pass_sign(z, c->p.Cav);
@@ -1099,7 +1136,11 @@ int mpc_linearstep(mpc_ctx* c, double* A, const double* exp_D0, const double* ex
     TableSet t;
     if ((rc = alloc_tables(c, &t))) return rc;
     cudaError_t e = cudaMemcpyAsync(t.f64, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice, c->st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess && (rc = field_copy(c, c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D field"))) {
+        cudaStreamSynchronize(c->st);
+        cudaFree(t.f64);
+        return rc;
+    }
     if (e == cudaSuccess && (rc = split_tables(c, t))) {
         cudaStreamSynchronize(c->st);
         cudaFree(t.f64);
@@ -1117,9 +1158,9 @@ int mpc_linearstep(mpc_ctx* c, double* A, const double* exp_D0, const double* ex
     rc = launch_pencil(c, mpc::PM_ENTRY_C128, a);
     if (!rc) rc = launch_plane(c, c->S, c->S, t, nullptr);
     if (!rc) rc = exit_to_io(c, 0);
+    if (!rc) rc = field_copy(c, A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, "D2H field");
     if (!rc) {
-        e = cudaMemcpyAsync(A, c->io, sizeof(double2) * c->N, cudaMemcpyDeviceToHost, c->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        e = cudaStreamSynchronize(c->st);
         if (e != cudaSuccess) rc = fail(MPC_ERR_CUDA, "linearstep", e);
     }
     cudaStreamSynchronize(c->st);
@@ -1155,7 +1196,7 @@ int mpc_ioniz(mpc_ctx* c, const double* A, double* tau_c, double* fe_sp) {
     int rc = ensure_io(c, 0);
     if (rc) return rc;
     if ((rc = ensure_io(c, 1))) return rc;
-    CK(cudaMemcpyAsync(c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D field");
+    if ((rc = field_copy(c, c->io, A, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D field"))) return rc;
     PencilArgs a{};
     a.in = c->io;
     a.in_scale = c->fs;
@@ -1166,8 +1207,8 @@ int mpc_ioniz(mpc_ctx* c, const double* A, double* tau_c, double* fe_sp) {
     a.tau_out = tau_d;
     a.fe_out = fe_d;
     if ((rc = launch_pencil(c, mpc::PM_IONIZ, a))) return rc;
-    CK(cudaMemcpyAsync(tau_c, tau_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H tau_c");
-    CK(cudaMemcpyAsync(fe_sp, fe_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st), "D2H fe_sp");
+    if ((rc = field_copy(c, tau_c, tau_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, "D2H tau_c"))) return rc;
+    if ((rc = field_copy(c, fe_sp, fe_d, sizeof(double) * c->N, cudaMemcpyDeviceToHost, "D2H fe_sp"))) return rc;
     CK(cudaStreamSynchronize(c->st), "ioniz");
     return MPC_OK;
 }
@@ -1216,8 +1257,8 @@ int mpc_setStep(mpc_ctx* c, double* dzz, const double* C1, const double* C2, con
     int rc = ensure_io(c, 0);
     if (rc) return rc;
     if ((rc = ensure_io(c, 1))) return rc;
-    CK(cudaMemcpyAsync(c->io, C1, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D C1");
-    CK(cudaMemcpyAsync(c->io2, C2, sizeof(double2) * c->N, cudaMemcpyHostToDevice, c->st), "H2D C2");
+    if ((rc = field_copy(c, c->io, C1, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D C1"))) return rc;
+    if ((rc = field_copy(c, c->io2, C2, sizeof(double2) * c->N, cudaMemcpyHostToDevice, "H2D C2"))) return rc;
     CK(cudaMemsetAsync(c->dred, 0, 2 * sizeof(double), c->st), "memset");
     k_diffnorm_c128<<<c->nsm * 4, 256, 0, c->st>>>(c->io, c->io2, c->N, c->dred);
     CK(cudaGetLastError(), "k_diffnorm_c128");

@@ -105,6 +105,36 @@ def test_ioniz(gpu_lib):
     assert rel(fe, fe_ref) < 1e-6
 
 
+def test_pinned_host_buffers_move_by_sm_copies(gpu_lib):
+    """Upload, download and the reference-signature step through page-locked host buffers take the
+    SM copy kernel (one more launch per transfer) and give the same bits as pageable buffers (the
+    copy engine path)."""
+    from mpc_gb300.capi import PinnedArray, Propagator
+    p, A, o = small_cell()
+    pin_in, pin_out = PinnedArray(p.N), PinnedArray(p.N)
+    with Propagator(p) as prop:
+        n0 = prop.launch_count()
+        prop.upload(A)
+        n1 = prop.launch_count()
+        ref = prop.download()
+        n2 = prop.launch_count()
+        pin_in.array[:] = A
+        prop.upload(pin_in.array)
+        n3 = prop.launch_count()
+        prop.download(pin_out.array)
+        n4 = prop.launch_count()
+        assert (n3 - n2) == (n1 - n0) + 1 and (n4 - n3) == (n2 - n1) + 1
+        assert np.array_equal(pin_out.array, ref)
+        # one reference-signature step on a pageable and on a pinned copy of the same field
+        B = ref.copy()
+        prop.ssfmprop(B, p.dzz, 1, 0.0, p.puls_e)
+        pin_in.array[:] = ref
+        prop.ssfmprop(pin_in.array, p.dzz, 1, 0.0, p.puls_e)
+        assert np.array_equal(pin_in.array, B)
+    pin_in.free()
+    pin_out.free()
+
+
 @pytest.mark.parametrize("plasm,sst", [(1, 1), (0, 1), (1, 0), (0, 0)])
 def test_ssfmprop_one_step(gpu_lib, plasm, sst):
     from mpc_gb300.capi import Propagator

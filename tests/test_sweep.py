@@ -115,6 +115,53 @@ def test_batch_step_double_matches_cells_one_by_one(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_batch_cells_match_the_oracle(gpu_lib):
+    """Every cell of a batch against the FP64 oracle (not only against itself run alone): 7 fixed
+    split steps in one graph, then 4 step-doubling attempts as batch rounds, with the oracle's
+    accept/reject decisions, step sizes and z (propagation.c:111-372, 616-677; MPC.c:269-383)."""
+    import oracle
+    from mpc_gb300.capi import Batch, Propagator
+    cells = []
+    for c in _small_cells():
+        c.passes = 4                 # room for the 7 fixed steps and the 4 attempts
+        p, A = inputs.make_cell(c)
+        o = oracle.Oracle(p)
+        o.calibrate(A)
+        cells.append((p, A, o))
+    props = [Propagator(p) for p, _, _ in cells]
+    refs, states = [], []
+    for prop, (p, A, o) in zip(props, cells):
+        prop.upload(A)
+        ref = A.copy()
+        st = o.new_state()
+        o.run_fixed(ref, st, 7)
+        refs.append(ref)
+        states.append(st)
+    try:
+        with Batch(props) as b:
+            b.run_fixed(7)
+            for prop, ref in zip(props, refs):
+                got = prop.download()
+                assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+            scratch = [(np.empty_like(r), np.empty_like(r)) for r in refs]
+            for _ in range(4):
+                bad, err = b.step_double()
+                for i, ((p, A, o), ref, st, (C1, C2)) in enumerate(zip(cells, refs, states, scratch)):
+                    assert bad[i] >= 0          # no cell has finished its distance yet
+                    o.double_step(ref, C1, C2, st)
+                    assert int(bad[i]) == st.bad
+                    assert abs(err[i] / st.err - 1) < 0.05
+                    s = props[i].state()
+                    assert s.dzz == pytest.approx(st.dzz, rel=1e-12) and s.z == pytest.approx(st.z, rel=1e-12, abs=1e-15)
+        for prop, ref in zip(props, refs):
+            got = prop.download()
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+    finally:
+        for prop in props:
+            prop.close()
+
+
+@pytest.mark.gpu
 def test_sweep_runs_every_cell_to_its_distance(gpu_lib):
     cfgs = _small_cells()
     for c in cfgs:
