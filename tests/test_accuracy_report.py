@@ -182,6 +182,7 @@ def _adaptive_replay(cfg, label, passes=None, max_attempts=None):
         prop.upload(A)
         g.upload(A)
         st = g.new_state()
+        done_passes = 0
         while True:
             s = prop.state()
             if s.z >= dist - 1e-12 or (max_attempts and n_att >= max_attempts):
@@ -193,6 +194,13 @@ def _adaptive_replay(cfg, label, passes=None, max_attempts=None):
             n_acc += 1 - d["bad"]
             disagree += int(own_bad != d["bad"])
             max_rel_err_diff = max(max_rel_err_diff, abs(own_err - d["err"]) / own_err)
+            z = prop.state().z
+            if passes and z < dist - 1e-12 and int(z / cfg.cav + 1e-9) > done_passes:
+                # a pass completed: its figures now, so that a run stopped later keeps them
+                done_passes = int(z / cfg.cav + 1e-9)
+                _errors(prop.download(), g.download(), p, e0, f"{label}, after pass {done_passes}", attempts=n_att,
+                        accepted=n_acc, split_steps=3 * n_att, decisions_differing=disagree,
+                        max_rel_local_error_diff=max_rel_err_diff, z=z, wall_s=round(time.time() - t0, 1))
         got = prop.download()
         s = prop.state()
         ref = g.download()
