@@ -254,6 +254,33 @@ struct NoOp {
     static constexpr bool active = false;
 };
 
+// Warp-local tail.  The last two stages of a transform (sub-length L2 = 16 * Ll, then the span-1
+// stage of radix Ll) work inside sub-transforms of L2 points.  When a warp's 32 work items of the
+// stage L2 are exactly one such sub-transform (NL * Ll == 32 lines x butterflies) and the warps
+// share the sub-transforms evenly, the span-1 stage can give each warp the same sub-transforms it
+// had in stage L2: the barrier between the two stages is then a warp barrier (__syncwarp), and the
+// warps run the tail independently.  Used where those conditions hold (the 2048-point transforms of
+// 4-pencil tiles on 256 threads); per butterfly the arithmetic is unchanged.
+__host__ __device__ constexpr int tail_last(int N) { return N <= 16 ? N : tail_last(N / 16); }
+template <int N, int NL, int NTH>
+struct WarpTail {
+    static constexpr int LL = tail_last(N);      // radix (and length) of the span-1 stage
+    static constexpr int L2 = 16 * LL;           // sub-transform length of the tail
+    static constexpr int NW = NTH / 32;
+    static constexpr int PPS = 16 / LL;          // warp passes per sub-transform in the span-1 stage
+    static constexpr bool ok = N > L2 && NTH % 32 == 0 && NL * LL == 32 && 16 % LL == 0 &&
+                               ((N / 16) * NL) % NTH == 0 && (N / L2) % NW == 0 &&
+                               ((N / LL) * NL) % NTH == 0 && ((N / LL) * NL) / NTH == ((N / L2) / NW) * PPS;
+    // item (line, butterfly g) of pass u of the span-1 stage for thread tid
+    __device__ __forceinline__ static void item(int tid, int u, int& line, int& g) {
+        const int w = tid >> 5, lane = tid & 31;
+        const int sub = w + NW * (u / PPS);
+        const int i = (u % PPS) * 32 + lane;
+        line = i % NL;
+        g = sub * 16 + i / NL;
+    }
+};
+
 // DIF stage of sub-length L (span S = L/R): y_k = W_L^(j k) * sum_q x_q W_R^(q k).
 // NTH threads share the stage's TOT butterflies; UNR of a thread's butterflies are unrolled
 // together so that their shared-memory loads overlap.
@@ -263,10 +290,17 @@ __device__ __forceinline__ void dif_stage(float2* s, Twiddles tw, int tid, const
     constexpr int S = L / R;
     constexpr int NB = N / R;
     constexpr int TOT = NB * V::NLINES;
+    using WT = WarpTail<N, V::NLINES, NTH>;
+    constexpr bool WTAIL = WT::ok && S == 1;
 #pragma unroll UNR
     for (int idx = tid; idx < TOT; idx += NTH) {
-        const int line = idx % V::NLINES;
-        const int g = idx / V::NLINES;
+        int line, g;
+        if constexpr (WTAIL) {
+            WT::item(tid, (idx - tid) / NTH, line, g);
+        } else {
+            line = idx % V::NLINES;
+            g = idx / V::NLINES;
+        }
         const int b = g / S, j = g - (g / S) * S;
         float2* p0 = s + V::at(b * L + j, line);
         float2 v[R];
@@ -298,10 +332,17 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const
     constexpr int S = L / R;
     constexpr int NB = N / R;
     constexpr int TOT = NB * V::NLINES;
+    using WT = WarpTail<N, V::NLINES, NTH>;
+    constexpr bool WTAIL = WT::ok && S == 1;
 #pragma unroll UNR
     for (int idx = tid; idx < TOT; idx += NTH) {
-        const int line = idx % V::NLINES;
-        const int g = idx / V::NLINES;
+        int line, g;
+        if constexpr (WTAIL) {
+            WT::item(tid, (idx - tid) / NTH, line, g);
+        } else {
+            line = idx % V::NLINES;
+            g = idx / V::NLINES;
+        }
         const int b = g / S, j = g - (g / S) * S;
         float2* p0 = s + V::at(b * L + j, line);
         float2 v[R];
@@ -339,7 +380,9 @@ __device__ __forceinline__ void dit_stage(float2* s, Twiddles tw, int tid, const
 template <int N, int L, class V, int NTH, int UNR = 1, class SINK = NoOp>
 __device__ __forceinline__ void dif_all(float2* s, Twiddles tw, int tid, const SINK& sink = SINK{}) {
     dif_stage<N, L, V, NTH, UNR, SINK>(s, tw, tid, sink);
-    __syncthreads();
+    using WT = WarpTail<N, V::NLINES, NTH>;
+    if constexpr (WT::ok && L == WT::L2) __syncwarp();   // the span-1 stage stays inside the warp
+    else __syncthreads();
     constexpr int R = Radix<L>::R;
     if constexpr (L / R > 1) dif_all<N, L / R, V, NTH, UNR, SINK>(s, tw, tid, sink);
 }
@@ -351,7 +394,9 @@ __device__ __forceinline__ void dit_all(float2* s, Twiddles tw, int tid, const S
     constexpr int R = Radix<L>::R;
     if constexpr (L / R > 1) dit_all<N, L / R, V, NTH, UNR, CORR, SRC, SINK>(s, tw, tid, src, sink);
     dit_stage<N, L, V, NTH, UNR, CORR, SRC, SINK>(s, tw, tid, src, sink);
-    __syncthreads();
+    using WT = WarpTail<N, V::NLINES, NTH>;
+    if constexpr (WT::ok && L == WT::LL) __syncwarp();   // stage L2 reads only this warp's results
+    else __syncthreads();
 }
 
 // Forward transform, a diagonal operator in position order, inverse transform: the span-1 stage

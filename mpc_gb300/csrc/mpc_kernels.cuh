@@ -110,15 +110,19 @@ struct PencilArgs {
 //   (u, v)_{k+1} = (u_k + c2_k v_k, g_k - u_k)     map (M, o): x -> M x + o
 // with a_k = W1 Kon, b_k = Wava Kon, c2_k = W2 Kon, g_k = 1 - exp(-R_k); u = ions2,
 // v = ions1, both zero before the first slice; fe_sp[k] = (v_k + 2 u_k) sigma_k.
-// Chunk maps are composed in FP32 inside a thread's CH points and across chunks in FP64.
+// Chunk maps are composed in FP32 inside a thread's CH points and across chunks in FP64.  Across
+// chunks the R map is held as (D, C) = (1 - B, C), R -> D R + C, so that composing two maps is one
+// FP64 product and one FP64 FMA (GB300 issues FP64 at 1/64 of its FP32 rate).  D keeps 1 - B to
+// FP64's absolute precision (1e-16), which is what the product D R needs; B's own relative
+// precision does not enter.
 // ---------------------------------------------------------------------------------------
-struct MapR { double B, C; };
+struct MapR { double D, C; };
 struct MapUV { double m00, m01, m10, m11, o0, o1; };
 
 __device__ __forceinline__ MapR compose(const MapR& first, const MapR& then) {
     MapR r;
-    r.B = first.B + then.B - first.B * then.B;
-    r.C = (1.0 - then.B) * first.C + then.C;
+    r.D = then.D * first.D;
+    r.C = fma(then.D, first.C, then.C);
     return r;
 }
 __device__ __forceinline__ MapUV compose(const MapUV& f, const MapUV& t) {
@@ -134,7 +138,7 @@ __device__ __forceinline__ MapUV compose(const MapUV& f, const MapUV& t) {
 template <class M>
 __device__ __forceinline__ M map_ident();
 template <>
-__device__ __forceinline__ MapR map_ident<MapR>() { return MapR{0.0, 0.0}; }
+__device__ __forceinline__ MapR map_ident<MapR>() { return MapR{1.0, 0.0}; }
 template <>
 __device__ __forceinline__ MapUV map_ident<MapUV>() { return MapUV{1.0, 0.0, 0.0, 1.0, 0.0, 0.0}; }
 
@@ -316,7 +320,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
                 B = fmaf(-B, ip.b, B + ip.b);
                 any2 |= ip.second;
             }
-            mr[p * TPP + ch] = MapR{(double)B, (double)C};
+            mr[p * TPP + ch] = MapR{1.0 - (double)B, (double)C};
         }
         any2 = __syncthreads_or(any2);
         scan_chunks<MapR, P, TPP>(mr, tid);   // carries across chunks in FP64

@@ -204,28 +204,82 @@ def _wavefronts(addrs):
     return max(len(r) for r in rows.values())
 
 
+def _warp_tail(N, NL, NTH):
+    """mpc_fft.cuh WarpTail: whether the span-1 stage keeps each warp on the sub-transforms of
+    the stage before, and its (line, butterfly) of pass u for thread tid."""
+    LL = N
+    while LL > 16:
+        LL //= 16
+    L2, NW, PPS = 16 * LL, NTH // 32, max(1, 16 // LL)
+    ok = (N > L2 and NTH % 32 == 0 and NL * LL == 32 and 16 % LL == 0 and (N // 16 * NL) % NTH == 0
+          and (N // L2) % NW == 0 and (N // LL * NL) % NTH == 0 and (N // LL * NL) // NTH == (N // L2) // NW * PPS)
+
+    def item(tid, u):
+        w, lane = tid >> 5, tid & 31
+        sub = w + NW * (u // PPS)
+        i = (u % PPS) * 32 + lane
+        return i % NL, sub * 16 + i // NL
+    return ok, LL, L2, item
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 def test_pencil_view_bank_conflict_free(shape):
     """Every FFT stage of the pencil tile and the CH-sample t walk of the nonlinear step take
-    the minimum two wavefronts per warp access (no bank conflicts)."""
+    the minimum two wavefronts per warp access (no bank conflicts); the span-1 stage with the
+    warp-local mapping where it applies."""
     name, N, P, at, size = _views(*shape)[0]
     CH = shape[6]
     nthr = N * P // CH
+    ok, LL, _, item = _warp_tail(N, P, nthr)
     L = N
     while L > 1:
         R = 16 if L >= 16 else L
         S = L // R
-        for w0 in range(0, min(N // R * P, nthr), 32):
-            for q in range(R):
-                addrs = []
-                for idx in range(w0, w0 + 32):
-                    line, g = idx % P, idx // P
-                    addrs.append(at((g // S) * L + g % S + S * q, line))
-                assert _wavefronts(addrs) <= 2, (shape, L, w0, q)
+        if ok and S == 1:
+            for w in range(nthr // 32):
+                for u in range(N // R * P // nthr):
+                    for q in range(R):
+                        addrs = []
+                        for tid in range(32 * w, 32 * w + 32):
+                            line, g = item(tid, u)
+                            addrs.append(at(g * L + q, line))
+                        assert _wavefronts(addrs) <= 2, (shape, L, w, u, q)
+        else:
+            for w0 in range(0, min(N // R * P, nthr), 32):
+                for q in range(R):
+                    addrs = []
+                    for idx in range(w0, w0 + 32):
+                        line, g = idx % P, idx // P
+                        addrs.append(at((g // S) * L + g % S + S * q, line))
+                    assert _wavefronts(addrs) <= 2, (shape, L, w0, q)
         L //= R
     for w0 in range(0, min(nthr, 256), 32):
         for i in range(CH):
             assert _wavefronts([at(CH * (t // P) + i, t % P) for t in range(w0, w0 + 32)]) <= 2, (shape, i)
+
+
+@pytest.mark.parametrize("N,NL,NTH", [(2048, 4, 256), (1024, 8, 256), (2048, 8, 512), (512, 32, 512)])
+def test_warp_tail_mapping(N, NL, NTH):
+    """Where the warp-local tail applies, its span-1 stage visits every (line, butterfly) once
+    and each warp works only inside the sub-transforms it wrote in the stage before (so a warp
+    barrier between the two stages suffices); the 2048-point, 4-pencil, 256-thread tile uses it."""
+    ok, LL, L2, item = _warp_tail(N, NL, NTH)
+    assert ok == ((N, NL, NTH) in [(2048, 4, 256), (1024, 8, 256)])
+    if not ok:
+        return
+    TOT = N // LL * NL
+    seen = set()
+    for tid in range(NTH):
+        w = tid >> 5
+        # stage L2 (radix 16, span LL), default mapping: the sub-transforms this warp wrote
+        mine = {((tid + u * NTH) // NL // LL) for u in range(N // 16 * NL // NTH)}
+        for u in range(TOT // NTH):
+            line, g = item(tid, u)
+            assert 0 <= line < NL and 0 <= g < N // LL
+            seen.add((line, g))
+            assert g * LL // L2 in mine, (tid, u)
+        assert all(b % (NTH // 32) == w for b in mine)
+    assert len(seen) == TOT
 
 
 def _xsw(x, l):
