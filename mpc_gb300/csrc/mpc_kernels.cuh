@@ -36,7 +36,17 @@ constexpr int kTilePoints = 16384;     // default pencil tile: P * Nt complex po
 #define MPC_PENCIL_UNROLL 4
 #endif
 constexpr int kPencilUnroll = MPC_PENCIL_UNROLL;
-constexpr int kDAPrefetch = 4;         // dA samples loaded ahead of use in the nonlinear walk
+// dA samples loaded ahead of use in the nonlinear walk, and the first walk's unroll (tuning builds
+// set them with MPC_NVCC_EXTRA, e.g. "-DMPC_DA_PREFETCH=8")
+#ifndef MPC_DA_PREFETCH
+#define MPC_DA_PREFETCH 4
+#endif
+#ifndef MPC_S1_UNROLL
+#define MPC_S1_UNROLL 8
+#endif
+constexpr int kDAPrefetch = MPC_DA_PREFETCH;
+constexpr int kS1Unroll = MPC_S1_UNROLL;
+static_assert(kDAPrefetch >= 1 && kDAPrefetch <= 32, "dA prefetch depth within a 32-sample chunk");
 
 // FP32 constants of the nonlinear step, computed on the host in FP64.
 struct NLConst {
@@ -312,7 +322,7 @@ __device__ __forceinline__ void nonlinear_tile(float2* s, const float2* __restri
         {
             float B = 0.0f, C = 0.0f;
             const float e2thr = ion_second_threshold(c);
-#pragma unroll 8
+#pragma unroll kS1Unroll
             for (int i = 0; i < CH; i++) {
                 const IonAB ip = ion_point_ab(w[V::walk(i)], c, e2thr);
                 const float Ck = fmaf(1.0f - ip.b, ip.a, ip.b);
