@@ -132,15 +132,15 @@ def profile_traffic(names):
 
 
 WORKLOADS = {
-    "cell256": dict(config="config2", adaptive=False, per_step=400, cpu_steps=5,
+    "cell256": dict(cell="cell256", adaptive=False, per_step=400, cpu_steps=5,
                     desc="multipass cell 256x256x2048, fixed split steps, lens mirror, SST + ADK + plasma on",
                     step="one pass of the cell = 400 split steps",
                     profile={"pencil": ["pencil_step_256x256x2048.txt"],
                              "plane": ["plane_y_tma_256x256x2048.txt", "plane_x_tma_256x256x2048.txt"]}),
-    "cell64": dict(config="config1", adaptive=False, per_step=200, cpu_steps=100,
+    "cell64": dict(cell="cell64", adaptive=False, per_step=200, cpu_steps=100,
                    desc="multipass cell 64x64x512, fixed split steps, lens mirror, SST + ADK + plasma on",
                    step="one pass of the cell = 200 split steps", profile=None),
-    "cell512": dict(config="config3", adaptive=True, per_step=10, cpu_steps=2,
+    "cell512": dict(cell="cell512", adaptive=True, per_step=10, cpu_steps=2,
                     desc="plasma-dominated cell 512x512x1024 (3 mJ, 120 fs, argon 3 bar), adaptive step "
                          "doubling at 1e-5, lens mirror, SST + ADK + plasma on",
                     step="10 step-doubling attempts = 30 split steps", profile=None),
@@ -149,7 +149,7 @@ WORKLOADS = {
 
 def make_workload(name: str = "cell256"):
     from mpc_gb300 import inputs
-    cfg = getattr(inputs, WORKLOADS[name]["config"])()
+    cfg = getattr(inputs, WORKLOADS[name]["cell"])()
     p, A = inputs.make_cell(cfg)
     return cfg, p, A
 

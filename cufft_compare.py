@@ -57,7 +57,7 @@ def time_cufft_linear(Nx: int, Ny: int, Nt: int, reps: int = 20) -> dict:
 def time_library(Nx: int, Ny: int, Nt: int, steps: int = 20, **physics) -> dict:
     from mpc_gb300 import inputs
     from mpc_gb300.capi import Propagator
-    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **physics)
+    cfg = inputs.cell256(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **physics)
     p, A = inputs.make_cell(cfg)
     with Propagator(p.copy(variant=-1)) as prop:
         prop.upload(A, calibrate=True)

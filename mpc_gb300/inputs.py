@@ -13,8 +13,9 @@ The reference reads these from an external preprocessor that is not part of it
              plus complex Gaussian noise of relative amplitude 1e-4 (splitmix64 + Box-Muller);
              Esig = sum |A|^2 dx dy dt hbar w0 of that seed, so MPC.c's calibration
              A *= sqrt(puls_e/Esig) gives the configured pulse energy.
-The benchmark workloads of the multipass-cell study are named configurations below; the
-data are synthetic stand-ins with the stated shapes and distributions.
+The benchmark workloads of the multipass-cell study are the named cells below (cell64, cell256,
+cell512, by their transverse grid); the data are synthetic stand-ins with the stated shapes and
+distributions.
 """
 from __future__ import annotations
 
@@ -131,19 +132,19 @@ def make_cell(cfg: CellConfig) -> tuple[MPCParams, np.ndarray]:
 
 
 # ---- the named workloads -------------------------------------------------------------
-def config1(**kw) -> CellConfig:
+def cell64(**kw) -> CellConfig:
     """64x64 over 4 mm, 512 over 2 ps, 0.2 mJ, argon 1 bar, 4 passes x 200 fixed steps."""
     return CellConfig(**{**dict(Nx=64, Ny=64, Nt=512, window_xy=4e-3, window_t=2e-12, energy=0.2e-3,
                                 seed=0, passes=4, steps_per_pass=200), **kw})
 
 
-def config2(**kw) -> CellConfig:
+def cell256(**kw) -> CellConfig:
     """256x256 over 8 mm, 2048 over 4 ps, 1.0 mJ, 8 passes x 400 fixed steps."""
     return CellConfig(**{**dict(Nx=256, Ny=256, Nt=2048, window_xy=8e-3, window_t=4e-12, energy=1.0e-3,
                                 seed=1, passes=8, steps_per_pass=400), **kw})
 
 
-def config3(**kw) -> CellConfig:
+def cell512(**kw) -> CellConfig:
     """512x512 over 8 mm, 1024 over 2 ps, 3 mJ, 120 fs, argon 3 bar, 12 passes, adaptive 1e-5."""
     return CellConfig(**{**dict(Nx=512, Ny=512, Nt=1024, window_xy=8e-3, window_t=2e-12, energy=3e-3,
                                 fwhm=120e-15, pressure=3.0, seed=2, passes=12, steps_per_pass=400,
@@ -184,10 +185,11 @@ def write_run(cfg: CellConfig, datadir: str, nrun: int = 0) -> MPCParams:
 
 
 def main(argv=None) -> int:
-    """python -m mpc_gb300.inputs --config 1 --datadir DIR [--nrun N] [--set key=value ...]"""
+    """python -m mpc_gb300.inputs --cell 64 --datadir DIR [--nrun N] [--set key=value ...]"""
     import argparse
     ap = argparse.ArgumentParser(description="write param.bin, datar.bin and datai.bin for one cell")
-    ap.add_argument("--config", type=int, default=1, choices=[1, 2, 3])
+    ap.add_argument("--cell", type=int, default=64, choices=[64, 256, 512],
+                    help="64: 64x64x512, 256: 256x256x2048, 512: 512x512x1024 (adaptive)")
     ap.add_argument("--datadir", required=True, help="run directory prefix (the field goes here, "
                                                      "param.bin into DATADIR%%04d)")
     ap.add_argument("--nrun", type=int, default=0)
@@ -201,7 +203,7 @@ def main(argv=None) -> int:
             ap.error(f"unknown cell field {k}")
         typ = type(getattr(CellConfig(), k))
         kw[k] = typ(float(v)) if typ in (int, float) else typ(v)
-    cfg = {1: config1, 2: config2, 3: config3}[a.config](**kw)
+    cfg = {64: cell64, 256: cell256, 512: cell512}[a.cell](**kw)
     p = write_run(cfg, a.datadir, a.nrun)
     print(f"wrote {a.datadir}{a.nrun:04d}/param.bin and {a.datadir}/datar.bin, datai.bin: "
           f"{p.Nx}x{p.Ny}x{p.Nt}, dist {p.dist} m, dzz {p.dzz} m")

@@ -79,7 +79,7 @@ def _gpu_oracle_fixed(p, A, nsteps):
 @pytest.fixture(scope="module")
 def cell64_run():
     """The 64x64x512 cell's whole run (4 passes x 200 fixed steps, lens mirror) on the CPU oracle."""
-    cfg = inputs.config1()
+    cfg = inputs.cell64()
     p, A, o = _cell(cfg)
     n = cfg.passes * cfg.steps_per_pass
     ref = A.copy()
@@ -111,7 +111,7 @@ def test_gpu_oracle_pinned_cell64_whole_run(gpu_lib, cell64_run):
 def test_gpu_oracle_pinned_128_and_step_doubling(gpu_lib):
     """128x128x1024 (an intermediate grid): 10 fixed steps, then three step-doubling attempts
     decided by each oracle's own rule, to 1e-12 (field, local error, step size)."""
-    cfg = inputs.config1(Nx=128, Ny=128, Nt=1024, window_xy=6e-3, window_t=3e-12, energy=1e-3, seed=5,
+    cfg = inputs.cell64(Nx=128, Ny=128, Nt=1024, window_xy=6e-3, window_t=3e-12, energy=1e-3, seed=5,
                          steps_per_pass=100)
     p, A, o = _cell(cfg)
     ref = A.copy()
@@ -137,7 +137,7 @@ def test_gpu_oracle_pinned_128_and_step_doubling(gpu_lib):
     assert r2 < 1e-12
 
 
-@pytest.mark.parametrize("name", ["config2", "config3"])
+@pytest.mark.parametrize("name", ["cell256", "cell512"])
 def test_large_cells_four_steps(gpu_lib, name):
     """Four split steps of the 256x256x2048 cell and of the plasma-dominated 512x512x1024 cell:
     the device path within the split-step tolerance of the CPU oracle, and the GPU oracle within
@@ -155,14 +155,14 @@ def test_large_cells_four_steps(gpu_lib, name):
     assert rg < 1e-12
 
 
-def test_config2_first_pass(gpu_lib):
+def test_cell256_first_pass(gpu_lib):
     """The 256x256x2048 cell's first pass (400 fixed steps, ending on the mirror), device path
     against the FP64 GPU oracle: within the 1e-4 whole-run target."""
-    cfg = inputs.config2()
+    cfg = inputs.cell256()
     p, A, _ = _cell(cfg)
     n = cfg.steps_per_pass
     ref, _ = _gpu_oracle_fixed(p, A, n)
-    r = _errors(_device_fixed(p, A, n), ref, p, float(np.sum(np.abs(A) ** 2)), "config2 first pass",
+    r = _errors(_device_fixed(p, A, n), ref, p, float(np.sum(np.abs(A) ** 2)), "cell256 first pass",
                 split_steps=n)
     assert r["field_rel_l2"] < 1e-4 and r["spectrum_rel_l2"] < 1e-4 and abs(r["energy_drift"]) < 1e-5
 
@@ -210,10 +210,10 @@ def _adaptive_replay(cfg, label, passes=None, max_attempts=None):
                    z_match=bool(z_match), wall_s=round(time.time() - t0, 1))
 
 
-def test_config3_adaptive_replay(gpu_lib):
+def test_cell512_adaptive_replay(gpu_lib):
     """The plasma-dominated 512x512x1024 cell under step doubling at tolerance 1e-5: eight
     attempts, the FP64 GPU oracle following the device's step sizes and decisions."""
-    r = _adaptive_replay(inputs.config3(), "config3 adaptive, 8 attempts", max_attempts=8)
+    r = _adaptive_replay(inputs.cell512(), "cell512 adaptive, 8 attempts", max_attempts=8)
     assert r["z_match"] and r["decisions_differing"] == 0
     assert r["max_rel_local_error_diff"] < 1e-2
     assert r["field_rel_l2"] < 1e-5 and r["spectrum_rel_l2"] < 1e-5
@@ -223,28 +223,28 @@ WHOLE = pytest.mark.skipif(os.environ.get("MPC_WHOLE_RUNS") != "1", reason="whol
 
 
 @WHOLE
-def test_whole_run_config2(gpu_lib):
+def test_whole_run_cell256(gpu_lib):
     """The 256x256x2048 cell's whole run: 1 mJ, 8 passes x 400 fixed steps, lens mirror (3,200
     split steps), device path against the FP64 GPU oracle: the 1e-4 target."""
-    cfg = inputs.config2()
+    cfg = inputs.cell256()
     p, A, _ = _cell(cfg)
     n = cfg.passes * cfg.steps_per_pass
     t0 = time.time()
     ref, _ = _gpu_oracle_fixed(p, A, n)
     t1 = time.time()
     got = _device_fixed(p, A, n)
-    r = _errors(got, ref, p, float(np.sum(np.abs(A) ** 2)), "config2 whole run", split_steps=n,
+    r = _errors(got, ref, p, float(np.sum(np.abs(A) ** 2)), "cell256 whole run", split_steps=n,
                 oracle_s=round(t1 - t0, 1), device_s=round(time.time() - t1, 1))
     assert r["field_rel_l2"] < 1e-4
 
 
 @WHOLE
-def test_whole_run_config3(gpu_lib):
+def test_whole_run_cell512(gpu_lib):
     """The 512x512x1024 cell (3 mJ, 120 fs, argon 3 bar) under step doubling at 1e-5 for
     MPC_WHOLE_RUN_PASSES passes (all 12 by default), device path against the FP64 GPU oracle
     following its steps."""
-    cfg = inputs.config3()
+    cfg = inputs.cell512()
     passes = int(os.environ.get("MPC_WHOLE_RUN_PASSES", cfg.passes))
-    r = _adaptive_replay(cfg, f"config3 adaptive, {passes} passes", passes=passes)
+    r = _adaptive_replay(cfg, f"cell512 adaptive, {passes} passes", passes=passes)
     assert r["z_match"]
     assert r["field_rel_l2"] < 1e-4

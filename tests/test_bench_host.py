@@ -51,7 +51,7 @@ def test_workloads_name_existing_cells(bench):
     from mpc_gb300 import inputs
     assert "cell256" in bench.WORKLOADS
     for name, wl in bench.WORKLOADS.items():
-        cfg = getattr(inputs, wl["config"])()
+        cfg = getattr(inputs, wl["cell"])()
         assert cfg.Nx * cfg.Ny * cfg.Nt > 0 and wl["per_step"] > 0 and wl["cpu_steps"] > 0, name
     assert bench.WORKLOADS["cell512"]["adaptive"] and not bench.WORKLOADS["cell256"]["adaptive"]
 

@@ -15,7 +15,7 @@ def _cell(**kw):
     base = dict(Nx=32, Ny=32, Nt=256, window_xy=4e-3, window_t=2e-12, energy=2e-3, fwhm=150e-15, pressure=2.0,
                 cav=0.05, passes=2, steps_per_pass=5, def_err=3e-4, Ab_M=0.9)
     base.update(kw)
-    return inputs.config1(**base)
+    return inputs.cell64(**base)
 
 
 def test_generator_writes_reference_layout(tmp_path):

@@ -22,7 +22,7 @@ def rel(a, b):
 def small_cell(**kw):
     base = dict(Nx=32, Ny=32, Nt=256, window_xy=4e-3, window_t=2e-12, energy=0.5e-3, steps_per_pass=50)
     base.update(kw)
-    p, A = inputs.make_cell(inputs.config1(**base))
+    p, A = inputs.make_cell(inputs.cell64(**base))
     o = oracle.Oracle(p)
     o.calibrate(A)
     return p, A, o
@@ -225,7 +225,7 @@ def test_create_destroy_leaves_no_pending_error(gpu_lib):
     cudart = ctypes.CDLL("libcudart.so.13")      # the instance the library already loaded
     cudart.cudaGetLastError.restype = ctypes.c_int
     cudart.cudaGetLastError()
-    p, A = inputs.make_cell(inputs.config1(Nx=32, Ny=32, Nt=256))
+    p, A = inputs.make_cell(inputs.cell64(Nx=32, Ny=32, Nt=256))
     with Propagator(p) as prop:
         prop.ssfmprop(A.copy(), p.dzz, 1, 0.0, p.puls_e, change=1)
     assert cudart.cudaGetLastError() == 0
@@ -243,7 +243,7 @@ def test_kernel_variants_agree(gpu_lib, grid, bounce):
     from mpc_gb300.capi import MPCError, Propagator
     Nx, Ny, Nt = grid
     extra = dict(cav=0.5 / 400 * 5, steps_per_pass=5, bounce=BOUNCE_LENS) if bounce else {}
-    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **extra)
+    cfg = inputs.cell256(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, **extra)
     p0, A = inputs.make_cell(cfg)
     ref = None
     v = 0
@@ -277,7 +277,7 @@ def test_step_double_variants_agree(gpu_lib, grid):
     arithmetic)."""
     from mpc_gb300.capi import MPCError, Propagator
     Nx, Ny, Nt = grid
-    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, def_err=1e-5)
+    cfg = inputs.cell256(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048, def_err=1e-5)
     p0, A = inputs.make_cell(cfg)
     ref = None
     v = 0
@@ -483,7 +483,7 @@ def test_production_grids_match_oracle(gpu_lib, grid):
     lens mirror, SST + ADK + plasma) against the FP64 oracle: the split-step tolerance."""
     from mpc_gb300.capi import Propagator
     Nx, Ny, Nt = grid
-    cfg = inputs.config2(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048,
+    cfg = inputs.cell256(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=8e-3 * Nx / 256, window_t=4e-12 * Nt / 2048,
                          energy=1e-3, bounce=BOUNCE_LENS)
     p, A = inputs.make_cell(cfg)
     o = oracle.Oracle(p)

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_param_bin_roundtrip(tmp_path):
-    p, A = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32))
+    p, A = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=32))
     path = tmp_path / "param.bin"
     p.write(str(path))
     raw = path.read_bytes()
@@ -33,7 +33,7 @@ def test_param_bin_roundtrip(tmp_path):
 
 
 def test_param_bin_rejects_truncated():
-    p, _ = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32))
+    p, _ = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=32))
     with pytest.raises(Exception):
         MPCParams.from_bytes(p.to_bytes()[:-20])
 
@@ -45,10 +45,10 @@ def test_splitmix64_known_values():
 
 
 def test_generator_deterministic_and_calibrated():
-    p1, A1 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=5))
-    p2, A2 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=5))
+    p1, A1 = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=32, seed=5))
+    p2, A2 = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=32, seed=5))
     np.testing.assert_array_equal(A1, A2)
-    _, A3 = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=32, seed=6))
+    _, A3 = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=32, seed=6))
     assert not np.array_equal(A1, A3)
     HBAR = 1.054560652926899e-34
     E = np.sum(np.abs(A1) ** 2) * p1.dr ** 2 * p1.deltat * HBAR * p1.w0

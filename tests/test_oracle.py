@@ -32,7 +32,7 @@ def test_fft_vs_numpy(dims):
 
 
 def linear_cell(**kw):
-    cfg = inputs.config1(**{**dict(Nx=64, Ny=64, Nt=64, window_t=2e-12, noise=0.0, sst_on=0, plasm=0), **kw})
+    cfg = inputs.cell64(**{**dict(Nx=64, Ny=64, Nt=64, window_t=2e-12, noise=0.0, sst_on=0, plasm=0), **kw})
     p, A = inputs.make_cell(cfg)
     return cfg, p, A
 
@@ -97,7 +97,7 @@ def test_spm_phase_exact():
 
 @pytest.mark.parametrize("sst", [0, 1])
 def test_energy_conserved_without_plasma(sst):
-    cfg = inputs.config1(Nx=32, Ny=32, Nt=128, window_t=1e-12, energy=1e-3, plasm=0, sst_on=sst, steps_per_pass=20)
+    cfg = inputs.cell64(Nx=32, Ny=32, Nt=128, window_t=1e-12, energy=1e-3, plasm=0, sst_on=sst, steps_per_pass=20)
     p, A = inputs.make_cell(cfg)
     o = oracle.Oracle(p)
     o.calibrate(A)
@@ -109,7 +109,7 @@ def test_energy_conserved_without_plasma(sst):
 
 
 def test_plasma_absorbs_energy():
-    cfg = inputs.config1(Nx=32, Ny=32, Nt=128, window_t=1e-12, energy=3e-3, fwhm=100e-15, beam_w=0.15e-3,
+    cfg = inputs.cell64(Nx=32, Ny=32, Nt=128, window_t=1e-12, energy=3e-3, fwhm=100e-15, beam_w=0.15e-3,
                          pressure=3.0, steps_per_pass=20)
     p, A = inputs.make_cell(cfg)
     o = oracle.Oracle(p)
@@ -155,7 +155,7 @@ def test_adk_closed_form():
 def test_ionization_grows_forward_in_time():
     """Corrected prefix (A15): the free-electron density is non-decreasing along t on axis
     (the scan runs from the leading edge); as written it runs from the trailing edge."""
-    cfg = inputs.config1(Nx=16, Ny=16, Nt=256, window_t=1e-12, energy=3e-3, fwhm=80e-15, beam_w=0.1e-3,
+    cfg = inputs.cell64(Nx=16, Ny=16, Nt=256, window_t=1e-12, energy=3e-3, fwhm=80e-15, beam_w=0.1e-3,
                          pressure=3.0, noise=0.0)
     p, A = inputs.make_cell(cfg)
     o = oracle.Oracle(p)
@@ -181,7 +181,7 @@ def test_step_doubling_order():
     """Local error of the symmetric split step is O(dz^3): halving dz divides the
     step-doubling error estimate by ~8; Richardson's (4 C2 - C1)/3 is closer to a
     fine-step reference than C2."""
-    cfg = inputs.config1(Nx=16, Ny=16, Nt=128, window_t=1e-12, window_xy=2e-3, energy=2e-3, beam_w=0.2e-3,
+    cfg = inputs.cell64(Nx=16, Ny=16, Nt=128, window_t=1e-12, window_xy=2e-3, energy=2e-3, beam_w=0.2e-3,
                          plasm=0, sst_on=0, steps_per_pass=4)
     p, A = inputs.make_cell(cfg)
     p = p.copy(def_err=1.0)          # accept every attempt
@@ -211,7 +211,7 @@ def test_step_doubling_order():
 def test_lens_mode_vs_abcd():
     """Linear propagation through the cell with the mirror lens at each bounce follows the
     ABCD law for the Gaussian q parameter (free space L, then thin lens f = R/2)."""
-    cfg = inputs.config1(Nx=128, Ny=128, Nt=4, window_xy=8e-3, window_t=2e-12, fwhm=1e-9, noise=0.0, sst_on=0,
+    cfg = inputs.cell64(Nx=128, Ny=128, Nt=4, window_xy=8e-3, window_t=2e-12, fwhm=1e-9, noise=0.0, sst_on=0,
                          plasm=0, steps_per_pass=25, bounce=BOUNCE_LENS, roc=0.3, cav=0.5, beam_w=0.5e-3)
     p, A = inputs.make_cell(cfg)
     p = p.copy(gamma2=0.0, betas=np.zeros(p.Nt))

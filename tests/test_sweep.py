@@ -59,11 +59,11 @@ def test_shard_agrees_across_gloo_ranks():
 
 
 def _small_cells():
-    return [inputs.config1(Nx=16, Ny=16, Nt=64, window_xy=2e-3, window_t=1e-12, energy=0.3e-3, steps_per_pass=10,
+    return [inputs.cell64(Nx=16, Ny=16, Nt=64, window_xy=2e-3, window_t=1e-12, energy=0.3e-3, steps_per_pass=10,
                            passes=1, seed=5),
-            inputs.config1(Nx=32, Ny=32, Nt=256, window_xy=4e-3, window_t=2e-12, energy=1e-3, steps_per_pass=10,
+            inputs.cell64(Nx=32, Ny=32, Nt=256, window_xy=4e-3, window_t=2e-12, energy=1e-3, steps_per_pass=10,
                            passes=1, seed=6, pressure=2.0),
-            inputs.config1(Nx=64, Ny=64, Nt=512, steps_per_pass=10, passes=1, seed=7)]
+            inputs.cell64(Nx=64, Ny=64, Nt=512, steps_per_pass=10, passes=1, seed=7)]
 
 
 @pytest.mark.gpu

@@ -25,7 +25,7 @@ def rel(a, b):
 
 def _cell(Nx, Ny, Nt):
     # the 32x32x256 cell's sample spacings, 3 mJ, 120 fs, argon 3 bar (strong ionization)
-    cfg = inputs.config1(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=4e-3 * Nx / 32, window_t=2e-12 * Nt / 256, energy=3e-3,
+    cfg = inputs.cell64(Nx=Nx, Ny=Ny, Nt=Nt, window_xy=4e-3 * Nx / 32, window_t=2e-12 * Nt / 256, energy=3e-3,
                          fwhm=120e-15, pressure=3.0, beam_w=0.3e-3)
     p, A = inputs.make_cell(cfg)
     p = p.copy(betas=np.zeros(p.Nt), wr=np.zeros(p.Ny), alpha=0.0)
@@ -80,7 +80,7 @@ def test_nonlinear_noalloc_every_length(gpu_lib, Nt):
 def test_nonlinear_noalloc_rejects_oversize(gpu_lib):
     torch = pytest.importorskip("torch")
     from mpc_gb300.capi import nonlinear_noalloc
-    p, _ = inputs.make_cell(inputs.config1(Nx=16, Ny=16, Nt=64))
+    p, _ = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=64))
     big = p.copy(dims=(16, 16, 4096), w=np.zeros(4096), betas=np.zeros(4096))
     host = np.full(16 * 16 * 4096, 1 + 2j, dtype=np.complex64)
     buf = torch.from_numpy(host).to("cuda")       # a copy, no torch kernel
