@@ -83,6 +83,18 @@ def test_calc1oes():
         np.testing.assert_array_equal(yy, y)
 
 
+def test_library_calc1oes_matches_reference_vectors():
+    """The library's own host-side calc1oes (mpc_calc1oes, the beam-size search used after every
+    accepted step) against the vectors generated from the reference's code; no GPU call."""
+    from mpc_gb300 import build, capi
+    build.build()
+    r = G["c1_r"]
+    for BP, bps, y in zip(G["c1_BP"], G["c1_bps"], G["c1_y"]):
+        v, yy = capi.calc1oes(BP, r)
+        assert v == bps
+        np.testing.assert_array_equal(yy, y)
+
+
 def test_setStep():
     C1 = G["ss_C1"]
     noise = G["ss_noise"]
