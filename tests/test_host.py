@@ -392,6 +392,19 @@ def test_capi_library_exports_every_header_symbol():
     assert lib.mpc_shape_supported(100, 100, 100) == 0
 
 
+def test_context_without_a_gpu_fails_loudly():
+    """With no usable GPU, creating a context returns an error status with the CUDA reason
+    (raised as MPCError by the binding): there is no CPU fallback in the product."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from mpc_gb300 import build, capi, inputs
+    build.build()
+    p, _ = inputs.make_cell(inputs.cell64(Nx=16, Ny=16, Nt=64))
+    with pytest.raises(capi.MPCError, match="mpc_create: MPC_ERR_CUDA"):
+        capi.Propagator(p)
+
+
 def _tw_stage_offset(N, L):
     """Python statement of tw_stage_offset (mpc_fft.cuh): entries before the stage of sub-length L."""
     off, M = 0, N
