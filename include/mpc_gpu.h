@@ -246,9 +246,10 @@ int mpc_batch_stats(mpc_batch *batch, long *graphs, long *nodes);
 
 /* ---- measurement and host buffers (no counterpart in the reference) ---------------- */
 /* Page-locked host buffer for fast host<->device copies of the field.  Field-sized transfers
- * to or from page-locked, device-mapped, 16-byte aligned host memory (this allocator,
- * cudaMallocHost, cudaHostRegister) are done by the library's SM copy kernel, at the host
- * link's rate in every call; other host memory goes through cudaMemcpyAsync. */
+ * to or from page-locked, 16-byte aligned host memory mapped for the context's device (this
+ * allocator, cudaMallocHost or cudaHostRegister called while that device is current) are done
+ * by the library's SM copy kernel, at the host link's rate in every call; other host memory
+ * goes through cudaMemcpyAsync. */
 int mpc_host_alloc(void **ptr, size_t bytes);
 int mpc_host_free(void *ptr);
 /* The cudaStream_t every kernel of this context is launched on. */

@@ -342,6 +342,7 @@ struct mpc_ctx {
     ADKConst adk{};
     cudaStream_t st = nullptr;
     int nsm = 0, pencil_grid = 0, plane_clusters = 0;
+    int dev = 0;                // the device the context was created on
     float2* S = nullptr;        // state, slot layout
     float2* scratch = nullptr;
     double2* io = nullptr;      // complex128 staging, N
@@ -570,7 +571,8 @@ static int ensure_io(mpc_ctx* c, int which) {
 }
 
 // Field-sized host <-> device copies.  When the host buffer is page-locked and mapped into the
-// device's address space (cudaMallocHost, mpc_host_alloc, cudaHostRegister), SMs move it with
+// address space of the context's device (cudaMallocHost, mpc_host_alloc or cudaHostRegister while
+// that device was current), SMs move it with
 // 16-byte loads and stores over the host link: on GB300 that runs at the link's rate every time,
 // while a copy-engine transfer that follows a second or more without host-link traffic (the
 // normal case after a propagation pass) was measured at a third of it or less.  Pageable or
@@ -580,19 +582,20 @@ __global__ void k_host_copy(const float4* __restrict__ src, float4* __restrict__
         dst[i] = src[i];
 }
 
-// the device address of mapped page-locked host memory at p, or null
-static void* mapped_host(const void* p) {
+// the device address of page-locked host memory at p mapped for device dev (allocated or
+// registered while dev was current), or null
+static void* mapped_host(const void* p, int dev) {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+    return (at.type == cudaMemoryTypeHost && at.device == dev) ? at.devicePointer : nullptr;
 }
 
 static int field_copy(mpc_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, const char* what) {
     const void* host = kind == cudaMemcpyHostToDevice ? src : dst;
-    void* hdev = mapped_host(host);
+    void* hdev = mapped_host(host, c->dev);
     const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0) && bytes % 16 == 0;
     if (hdev && aligned && bytes > 0) {
         const float4* s = reinterpret_cast<const float4*>(kind == cudaMemcpyHostToDevice ? hdev : src);
@@ -687,6 +690,7 @@ int mpc_create(mpc_ctx** out, const mpc_params* p) {
     }
     int dev = 0;
     TRYC(cudaGetDevice(&dev), "cudaGetDevice");
+    c->dev = dev;
     TRYC(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
     TRYC(ops->setup(), "kernel attribute setup");
     TRYC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
