@@ -1115,7 +1115,7 @@ __global__ void __launch_bounds__(NTHR, strip_min_blocks(NTHR, MINB)) plane_y_ke
 }
 
 // y part with TMA staging: a persistent CTA walks its units (slot, strip of CXS columns) with
-// NBUF unit buffers in shared memory; one thread keeps NBUF - 1 units in flight as 2-D bulk tensor
+// NBUF unit buffers in shared memory; warp 0 keeps NBUF - 1 units in flight as 2-D bulk tensor
 // loads (box: CXS complex columns x NY rows of one omega-plane, landing in the StripYView layout)
 // plus a bulk copy of the slot's NY factors Ry(y) D(slot) (the slot-major table, 16 B each) on
 // the same mbarrier, and each finished unit leaves by a bulk tensor store, so no thread spends
