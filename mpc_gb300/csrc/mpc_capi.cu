@@ -572,11 +572,10 @@ static int ensure_io(mpc_ctx* c, int which) {
 
 // Field-sized host <-> device copies.  When the host buffer is page-locked and mapped into the
 // address space of the context's device (cudaMallocHost, mpc_host_alloc or cudaHostRegister while
-// that device was current), SMs move it with
-// 16-byte loads and stores over the host link: on GB300 that runs at the link's rate every time,
-// while a copy-engine transfer that follows a second or more without host-link traffic (the
-// normal case after a propagation pass) was measured at a third of it or less.  Pageable or
-// unaligned buffers go through cudaMemcpyAsync.
+// that device was current), SMs move it with 16-byte loads and stores over the host link: on
+// GB300 that runs at the link's rate every time, while a copy-engine transfer that follows a
+// second or more without host-link traffic (the normal case after a propagation pass) was
+// measured at a third of it or less.  Pageable or unaligned buffers go through cudaMemcpyAsync.
 __global__ void k_host_copy(const float4* __restrict__ src, float4* __restrict__ dst, size_t n) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         dst[i] = src[i];
